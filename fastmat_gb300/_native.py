@@ -1,0 +1,197 @@
+"""ctypes binding of the native engine's C ABI (include/fmgpu.h).
+
+The library is loaded lazily on first use.  If it is missing, or no CUDA
+device is present, every transform raises RuntimeError: there is no CPU
+fallback for the matvec path.
+"""
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+FM_OK = 0
+FM_ERR_VALUE = 1
+FM_ERR_TYPE = 2
+FM_ERR_UNSUPPORTED = 3
+FM_ERR_CUDA = 4
+FM_ERR_NOMEM = 5
+FM_ERR_TIMEOUT = 6
+
+# element types: fastmat's ftype numbering (fastmat/core/types.pxd:45-55)
+FM_I8, FM_I16, FM_I32, FM_I64, FM_F32, FM_F64, FM_C64, FM_C128 = range(8)
+DTYPE_CODE = {
+    np.dtype(np.int8): FM_I8, np.dtype(np.int16): FM_I16,
+    np.dtype(np.int32): FM_I32, np.dtype(np.int64): FM_I64,
+    np.dtype(np.float32): FM_F32, np.dtype(np.float64): FM_F64,
+    np.dtype(np.complex64): FM_C64, np.dtype(np.complex128): FM_C128,
+}
+CODE_DTYPE = {v: k for k, v in DTYPE_CODE.items()}
+
+(NODE_FOURIER, NODE_CIRCULANT, NODE_TOEPLITZ, NODE_HADAMARD, NODE_DIAG,
+ NODE_PARTIAL, NODE_PERMUTATION, NODE_PRODUCT, NODE_SUM, NODE_KRON,
+ NODE_HERMITIAN, NODE_CONJUGATE, NODE_EYE, NODE_DENSE) = range(1, 15)
+
+FORWARD = 0
+BACKWARD = 1
+
+
+class FmNode(ctypes.Structure):
+    _fields_ = [
+        ('kind', ctypes.c_int32), ('dtype', ctypes.c_int32),
+        ('rows', ctypes.c_int64), ('cols', ctypes.c_int64),
+        ('first_child', ctypes.c_int32), ('num_children', ctypes.c_int32),
+        ('n', ctypes.c_int64),
+        ('vec0', ctypes.c_void_p), ('len0', ctypes.c_int64),
+        ('type0', ctypes.c_int32), ('pad0', ctypes.c_int32),
+        ('vec1', ctypes.c_void_p), ('len1', ctypes.c_int64),
+        ('type1', ctypes.c_int32), ('pad1', ctypes.c_int32),
+        ('scalar_re', ctypes.c_double), ('scalar_im', ctypes.c_double),
+    ]
+
+
+class FmPlanInfo(ctypes.Structure):
+    _fields_ = [
+        ('rows', ctypes.c_int64), ('cols', ctypes.c_int64),
+        ('num_launches_fwd', ctypes.c_int32),
+        ('num_launches_bwd', ctypes.c_int32),
+        ('scratch_bytes_per_col', ctypes.c_int64),
+        ('const_bytes', ctypes.c_int64),
+        ('compute_type', ctypes.c_int32), ('pad', ctypes.c_int32),
+    ]
+
+
+#: every entry point include/fmgpu.h declares
+EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
+           'fm_execute_host',
+           'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
+           'fm_last_error', 'fm_version')
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libfmgpu.so (building it first if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError('fastmat_gb300 native library is not '
+                                   'built: %s' % path)
+            _build.build()
+        lib = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        I32, I64 = ctypes.c_int32, ctypes.c_int64
+        lib.fm_plan_create.argtypes = [ctypes.POINTER(FmNode), I32,
+                                       ctypes.POINTER(I32), I32, I32, I32,
+                                       ctypes.POINTER(P)]
+        lib.fm_plan_create.restype = ctypes.c_int
+        lib.fm_execute.argtypes = [P, I32, P, I32, I64, P, I32, I64, I64, P]
+        lib.fm_execute.restype = ctypes.c_int
+        lib.fm_execute_profiled.argtypes = [
+            P, I32, P, I32, I64, P, I32, I64, I64, P,
+            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I32)]
+        lib.fm_execute_profiled.restype = ctypes.c_int
+        lib.fm_execute_host.argtypes = [P, I32, P, I32, I64, P, I32, I64, I64]
+        lib.fm_execute_host.restype = ctypes.c_int
+        lib.fm_plan_destroy.argtypes = [P]
+        lib.fm_plan_destroy.restype = ctypes.c_int
+        lib.fm_plan_get_info.argtypes = [P, ctypes.POINTER(FmPlanInfo)]
+        lib.fm_plan_get_info.restype = ctypes.c_int
+        lib.fm_plan_describe.argtypes = [P, I32, ctypes.c_char_p, I64]
+        lib.fm_plan_describe.restype = ctypes.c_int
+        lib.fm_last_error.argtypes = []
+        lib.fm_last_error.restype = ctypes.c_char_p
+        lib.fm_version.argtypes = []
+        lib.fm_version.restype = I32
+        _lib = lib
+        return lib
+
+
+def check(status):
+    """Map a C ABI status to the exception fastmat raises for that case."""
+    if status == FM_OK:
+        return
+    msg = _lib.fm_last_error().decode(errors='replace') if _lib else ''
+    if status == FM_ERR_VALUE:
+        raise ValueError(msg)
+    if status == FM_ERR_TYPE:
+        raise TypeError(msg)
+    if status == FM_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if status == FM_ERR_NOMEM:
+        raise MemoryError(msg)
+    raise RuntimeError('fmgpu error %d: %s' % (status, msg))
+
+
+class Plan:
+    """Owns one native plan (an operator tree compiled for one compute
+    type)."""
+
+    def __init__(self, nodes, children, root, compute_type, keepalive):
+        lib = load()
+        n = len(nodes)
+        arr = (FmNode * n)(*nodes)
+        ch = (ctypes.c_int32 * max(1, len(children)))(*children)
+        handle = ctypes.c_void_p()
+        self._keep = keepalive
+        check(lib.fm_plan_create(arr, n, ch, len(children), root,
+                                 compute_type, ctypes.byref(handle)))
+        self.handle = handle
+        self.compute_type = compute_type
+        self._lib = lib
+
+    def execute(self, direction, x_ptr, x_type, ld_x, y_ptr, y_type, ld_y,
+                num_cols, stream):
+        check(self._lib.fm_execute(self.handle, direction, x_ptr, x_type,
+                                   ld_x, y_ptr, y_type, ld_y, num_cols,
+                                   stream))
+
+    def execute_profiled(self, direction, x_ptr, x_type, ld_x, y_ptr, y_type,
+                         ld_y, num_cols, stream):
+        """Run once, returning each launch's elapsed milliseconds."""
+        cap = 64
+        ms = (ctypes.c_float * cap)()
+        n = ctypes.c_int32(cap)
+        check(self._lib.fm_execute_profiled(
+            self.handle, direction, x_ptr, x_type, ld_x, y_ptr, y_type, ld_y,
+            num_cols, stream, ms, ctypes.byref(n)))
+        return [ms[i] for i in range(n.value)]
+
+    def execute_host(self, direction, x, y):
+        """x, y: Fortran-ordered 2-D numpy arrays (host memory)."""
+        check(self._lib.fm_execute_host(
+            self.handle, direction, x.ctypes.data, DTYPE_CODE[x.dtype],
+            x.shape[0], y.ctypes.data, DTYPE_CODE[y.dtype], y.shape[0],
+            x.shape[1]))
+
+    def info(self):
+        inf = FmPlanInfo()
+        check(self._lib.fm_plan_get_info(self.handle, ctypes.byref(inf)))
+        return inf
+
+    def describe(self, direction=FORWARD):
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(self._lib.fm_plan_describe(self.handle, direction, buf,
+                                         len(buf)))
+        return buf.value.decode()
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                self._lib.fm_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

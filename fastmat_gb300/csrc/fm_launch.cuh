@@ -1,0 +1,26 @@
+// Host-side launch entry points of the vector-program kernel, one per
+// compute element type (each defined in its own translation unit so the
+// five instantiations compile in parallel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fm_vprog.cuh"
+
+namespace fmk {
+
+cudaError_t launch_f32(const Step &st, int cls, int threads, size_t smem,
+                       i64 grid, cudaStream_t s);
+cudaError_t launch_f64(const Step &st, int cls, int threads, size_t smem,
+                       i64 grid, cudaStream_t s);
+cudaError_t launch_c64(const Step &st, int cls, int threads, size_t smem,
+                       i64 grid, cudaStream_t s);
+cudaError_t launch_c128(const Step &st, int cls, int threads, size_t smem,
+                       i64 grid, cudaStream_t s);
+cudaError_t launch_i64(const Step &st, int cls, int threads, size_t smem,
+                       i64 grid, cudaStream_t s);
+
+// maximum dynamic shared memory a launch may request (GB300: 227 KB / CTA)
+constexpr int kMaxSmem = 227 * 1024;
+
+}  // namespace fmk

@@ -1,0 +1,1465 @@
+// Planner and C ABI of the matvec engine.
+//
+// fm_plan_create lowers an operator tree (fm_node array, see fmgpu.h) into a
+// list of vector-program launches per direction:
+//   * every operator whose working vector fits in shared memory becomes a
+//     straight-line program over whole columns (Fourier: Stockham FFT;
+//     Circulant/Toeplitz: zero pad, FFT, spectrum multiply, inverse FFT,
+//     truncate; Bluestein Fourier: chirp, convolution, chirp; Hadamard: FWHT;
+//     Diag: multiply; Partial/Permutation: gathers), and adjacent programs
+//     of a Product chain are merged into one launch;
+//   * long transforms use the four-step decomposition N = N1 * N2 as two
+//     (FFT) or three (convolution) launches over strided views;
+//   * Kron applies each factor's program along its mode, in place;
+//   * Sum accumulates its terms into the output.
+// Device constants (twiddles, spectra, chirps, index maps) are computed on
+// the GPU in double precision and stored in the plan's compute type.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fmgpu.h"
+#include "fm_launch.cuh"
+
+using fmk::i64;
+typedef std::complex<double> cd;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &m) { throw Error{code, m}; }
+
+#define CUDA_TRY(x)                                                         \
+  do {                                                                      \
+    cudaError_t e_ = (x);                                                   \
+    if (e_ != cudaSuccess)                                                  \
+      fail(e_ == cudaErrorMemoryAllocation ? FM_ERR_NOMEM : FM_ERR_CUDA,    \
+           std::string(#x) + ": " + cudaGetErrorString(e_));                \
+  } while (0)
+
+int esize(int t) {
+  switch (t) {
+    case FM_I8: return 1;
+    case FM_I16: return 2;
+    case FM_I32: return 4;
+    case FM_I64: return 8;
+    case FM_F32: return 4;
+    case FM_F64: return 8;
+    case FM_C64: return 8;
+    case FM_C128: return 16;
+    default: return 0;
+  }
+}
+bool is_cplx(int t) { return t == FM_C64 || t == FM_C128; }
+bool valid_type(int t) { return t >= FM_I8 && t <= FM_C128; }
+
+cd host_get(const void *p, int t, i64 i) {
+  switch (t) {
+    case FM_I8: return cd(((const int8_t *)p)[i], 0);
+    case FM_I16: return cd(((const int16_t *)p)[i], 0);
+    case FM_I32: return cd(((const int32_t *)p)[i], 0);
+    case FM_I64: return cd((double)((const int64_t *)p)[i], 0);
+    case FM_F32: return cd(((const float *)p)[i], 0);
+    case FM_F64: return cd(((const double *)p)[i], 0);
+    case FM_C64: {
+      const float *f = (const float *)p + 2 * i;
+      return cd(f[0], f[1]);
+    }
+    case FM_C128: {
+      const double *f = (const double *)p + 2 * i;
+      return cd(f[0], f[1]);
+    }
+  }
+  fail(FM_ERR_TYPE, "unsupported element type");
+}
+
+i64 host_get_int(const void *p, int t, i64 i) {
+  switch (t) {
+    case FM_I8: return ((const int8_t *)p)[i];
+    case FM_I16: return ((const int16_t *)p)[i];
+    case FM_I32: return ((const int32_t *)p)[i];
+    case FM_I64: return ((const int64_t *)p)[i];
+    default: return (i64)host_get(p, t, i).real();
+  }
+}
+
+bool smooth(i64 n) {
+  if (n < 1) return false;
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+i64 next_pow2(i64 n) {
+  i64 p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+bool is_pow2(i64 n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ------------------------------------------------------------ helper kernels
+template <class E> __device__ E mk(double re, double im);
+template <> __device__ float mk<float>(double re, double) { return (float)re; }
+template <> __device__ double mk<double>(double re, double) { return re; }
+template <> __device__ i64 mk<i64>(double re, double) { return (i64)llrint(re); }
+template <> __device__ float2 mk<float2>(double re, double im) {
+  return make_float2((float)re, (float)im);
+}
+template <> __device__ double2 mk<double2>(double re, double im) {
+  return make_double2(re, im);
+}
+
+// tw[t] = exp(-2 pi i t / N); the phase t/N is exact in integers and the
+// only rounding is in double-precision sincospi.
+template <class E>
+__global__ void k_twiddle(E *tw, i64 N) {
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < N;
+       t += (i64)gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * (double)t / (double)N, &s, &c);
+    tw[t] = mk<E>(c, s);
+  }
+}
+
+// Bluestein chirp a[n] = exp(-i pi n^2 / N) with n^2 reduced mod 2N exactly
+__global__ void k_chirp(double2 *a, i64 N) {
+  for (i64 n = blockIdx.x * (i64)blockDim.x + threadIdx.x; n < N;
+       n += (i64)gridDim.x * blockDim.x) {
+    const i64 m = (n * n) % (2 * N);
+    double s, c;
+    sincospi(-(double)m / (double)N, &s, &c);
+    a[n] = make_double2(c, s);
+  }
+}
+
+// Bluestein filter h[m] = conj(a[|m|]) on the circle of length Lb
+__global__ void k_bluestein_filter(double2 *h, const double2 *a, i64 N,
+                                   i64 Lb) {
+  for (i64 m = blockIdx.x * (i64)blockDim.x + threadIdx.x; m < Lb;
+       m += (i64)gridDim.x * blockDim.x) {
+    double2 v = make_double2(0., 0.);
+    if (m < N) v = make_double2(a[m].x, -a[m].y);
+    else if (Lb - m < N) v = make_double2(a[Lb - m].x, -a[Lb - m].y);
+    h[m] = v;
+  }
+}
+
+// out[o] = scale * in[perm(o)] converted to E; perm for the four-step
+// layout: o = k1 * L2 + k2  <-  k1 + L1 * k2   (L1 == 0: identity)
+template <class E>
+__global__ void k_convert(E *out, const double2 *in, i64 n, double scale,
+                          i64 L1, i64 L2) {
+  for (i64 o = blockIdx.x * (i64)blockDim.x + threadIdx.x; o < n;
+       o += (i64)gridDim.x * blockDim.x) {
+    i64 src = o;
+    if (L1 > 0) {
+      const i64 k1 = o / L2, k2 = o - k1 * L2;
+      src = k1 + L1 * k2;
+    }
+    const double2 v = in[src];
+    out[o] = mk<E>(v.x * scale, v.y * scale);
+  }
+}
+
+int grid_for(i64 n) { return (int)std::min<i64>((n + 255) / 256, 4096); }
+
+// ------------------------------------------------------------ plan state
+struct LStep {
+  fmk::Step st;
+  int src, dst;  // 0 = x, 1 = y, >= 2 scratch
+  int cls, threads;
+  size_t smem;
+};
+
+}  // namespace
+
+struct fm_plan {
+  int ctype = FM_C128;
+  int esz = 16;
+  int device = 0;
+  i64 rows = 0, cols = 0;
+  std::vector<void *> allocs;
+  i64 const_bytes = 0;
+  std::map<i64, void *> twiddles;
+  std::vector<LStep> steps[2];
+  std::vector<i64> scratch_rows;  // rows per scratch buffer (id - 2)
+  // execution state
+  void *scratch = nullptr;
+  size_t scratch_cap = 0;
+  // host execution staging
+  void *dx = nullptr, *dy = nullptr;
+  size_t dx_cap = 0, dy_cap = 0;
+  cudaStream_t hstream = nullptr;
+  ~fm_plan();
+};
+
+fm_plan::~fm_plan() {
+  for (void *p : allocs) cudaFree(p);
+  if (scratch) cudaFree(scratch);
+  if (dx) cudaFree(dx);
+  if (dy) cudaFree(dy);
+  if (hstream) cudaStreamDestroy(hstream);
+}
+
+namespace {
+
+int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
+             void *y, int y_type, i64 ld_y, i64 M, cudaStream_t s,
+             std::vector<cudaEvent_t> *events = nullptr);
+
+// ------------------------------------------------------------ planner IR
+struct SStep {
+  fmk::View vin{1, 1, 1}, vout{1, 1, 1};
+  i64 in_rows = 0, out_rows = 0;
+  int L = 0, in_len = 0, out_len = 0;
+  std::vector<fmk::Op> ops;
+  int src = -1, dst = -2;  // -1 unit input, -2 unit output, k >= 0 temp k
+  const void *pre = nullptr, *post = nullptr;
+  int conj_in = 0, conj_out = 0;
+};
+
+struct Unit;
+typedef std::vector<Unit> Chain;
+
+struct Unit {
+  enum Kind { PROG, STEPS, SUM } kind = PROG;
+  i64 n_in = 0, n_out = 0;
+  // PROG
+  std::vector<fmk::Op> ops;
+  i64 L = 0;
+  // STEPS
+  std::vector<SStep> steps;
+  std::vector<i64> tmp_rows;
+  // SUM
+  std::vector<Chain> terms;
+};
+
+struct NodeRec {
+  fm_node d;
+  std::vector<int> ch;
+};
+
+fmk::Op mkop(int kind, int len) {
+  fmk::Op o;
+  memset(&o, 0, sizeof(o));
+  o.kind = kind;
+  o.len = len;
+  o.div = 1;
+  o.mod = 1;
+  o.stride = 0;
+  o.N = 1;
+  o.sre = 1.0;
+  return o;
+}
+
+class Planner {
+ public:
+  Planner(fm_plan *P, const std::vector<NodeRec> &nodes)
+      : P_(P), nodes_(nodes) {
+    cplx_ = is_cplx(P->ctype);
+    ept_ = P->esz >= 16 ? 8 : 16;
+    lmax_ = (i64)ept_ * FM_MAX_THREADS;
+  }
+
+  void build(int root) {
+    for (int dir = 0; dir < 2; ++dir) {
+      Chain c = compile(root, dir == FM_FORWARD);
+      const NodeRec &r = nodes_[root];
+      const i64 n_in = dir == FM_FORWARD ? r.d.cols : r.d.rows;
+      const i64 n_out = dir == FM_FORWARD ? r.d.rows : r.d.cols;
+      std::vector<LStep> &out = P_->steps[dir];
+      lower(c, 0, n_in, 1, n_out, out);
+      if (out.empty()) emit_copy(0, 1, n_in, out);
+    }
+  }
+
+ private:
+  fm_plan *P_;
+  const std::vector<NodeRec> &nodes_;
+  bool cplx_;
+  int ept_;
+  i64 lmax_;
+  std::map<const void *, std::vector<cd>> host_vec_;  // host copies of MUL
+  std::map<const void *, std::vector<i64>> host_map_;  // and GATHER data
+
+  // ---------------------------------------------------------- device data
+  void *dalloc(size_t bytes) {
+    void *p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    P_->allocs.push_back(p);
+    P_->const_bytes += (i64)bytes;
+    return p;
+  }
+
+  const void *twiddle(i64 N) {
+    auto it = P_->twiddles.find(N);
+    if (it != P_->twiddles.end()) return it->second;
+    void *p = dalloc((size_t)N * P_->esz);
+    if (P_->ctype == FM_C64)
+      k_twiddle<float2><<<grid_for(N), 256>>>((float2 *)p, N);
+    else
+      k_twiddle<double2><<<grid_for(N), 256>>>((double2 *)p, N);
+    CUDA_TRY(cudaGetLastError());
+    P_->twiddles[N] = p;
+    return p;
+  }
+
+  // upload a host vector in the compute type
+  const void *upload(const std::vector<cd> &v) {
+    const size_t n = v.size();
+    std::vector<unsigned char> buf(n * P_->esz);
+    for (size_t i = 0; i < n; ++i) {
+      switch (P_->ctype) {
+        case FM_F32: ((float *)buf.data())[i] = (float)v[i].real(); break;
+        case FM_F64: ((double *)buf.data())[i] = v[i].real(); break;
+        case FM_I64:
+          ((int64_t *)buf.data())[i] = (int64_t)llround(v[i].real());
+          break;
+        case FM_C64:
+          ((float *)buf.data())[2 * i] = (float)v[i].real();
+          ((float *)buf.data())[2 * i + 1] = (float)v[i].imag();
+          break;
+        default:
+          ((double *)buf.data())[2 * i] = v[i].real();
+          ((double *)buf.data())[2 * i + 1] = v[i].imag();
+          break;
+      }
+      if (!cplx_ && v[i].imag() != 0.0)
+        fail(FM_ERR_TYPE, "complex operator data in a real-valued plan");
+    }
+    void *p = dalloc(buf.size());
+    CUDA_TRY(cudaMemcpy(p, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    host_vec_[p] = v;
+    return p;
+  }
+
+  const i64 *upload_map(const std::vector<i64> &m) {
+    void *p = dalloc(m.size() * sizeof(i64));
+    CUDA_TRY(cudaMemcpy(p, m.data(), m.size() * sizeof(i64),
+                        cudaMemcpyHostToDevice));
+    host_map_[p] = m;
+    return (const i64 *)p;
+  }
+
+  std::vector<cd> node_vec(const fm_node &d, int which) {
+    const void *p = which == 0 ? d.vec0 : d.vec1;
+    const i64 n = which == 0 ? d.len0 : d.len1;
+    const int t = which == 0 ? d.type0 : d.type1;
+    std::vector<cd> v((size_t)n);
+    if (n > 0 && !p) fail(FM_ERR_VALUE, "missing operator data");
+    for (i64 i = 0; i < n; ++i) v[i] = host_get(p, t, i);
+    return v;
+  }
+  std::vector<i64> node_idx(const fm_node &d, int which) {
+    const void *p = which == 0 ? d.vec0 : d.vec1;
+    const i64 n = which == 0 ? d.len0 : d.len1;
+    const int t = which == 0 ? d.type0 : d.type1;
+    std::vector<i64> v((size_t)n);
+    for (i64 i = 0; i < n; ++i) v[i] = host_get_int(p, t, i);
+    return v;
+  }
+
+  // FFT of a length-L device c128 vector (L smooth), forward, in double,
+  // through a nested plan of this engine.
+  void fft_f64_device(const double2 *in, double2 *out, i64 L) {
+    fm_node nd;
+    memset(&nd, 0, sizeof(nd));
+    nd.kind = FM_NODE_FOURIER;
+    nd.dtype = FM_C128;
+    nd.rows = nd.cols = L;
+    nd.n = L;
+    std::vector<NodeRec> sub(1);
+    sub[0].d = nd;
+    fm_plan Q;
+    Q.ctype = FM_C128;
+    Q.esz = 16;
+    Q.device = P_->device;
+    Q.rows = Q.cols = L;
+    Planner(&Q, sub).build(0);
+    const int st = run_plan(&Q, FM_FORWARD, in, FM_C128, L, out, FM_C128, L,
+                            1, 0);
+    if (st != FM_OK) fail(st, "nested FFT failed: " + g_err);
+    CUDA_TRY(cudaDeviceSynchronize());
+  }
+
+  // spectrum fft(v)/L of a host vector (length L), in the compute type,
+  // optionally in the four-step (L1, L2) layout
+  const void *spectrum(const std::vector<cd> &v, i64 L1 = 0, i64 L2 = 0) {
+    const i64 L = (i64)v.size();
+    double2 *din = nullptr, *dout = nullptr;
+    CUDA_TRY(cudaMalloc(&din, L * sizeof(double2)));
+    CUDA_TRY(cudaMalloc(&dout, L * sizeof(double2)));
+    CUDA_TRY(cudaMemcpy(din, v.data(), L * sizeof(double2),
+                        cudaMemcpyHostToDevice));
+    fft_f64_device(din, dout, L);
+    const void *res = convert_dev(dout, L, 1.0 / (double)L, L1, L2);
+    cudaFree(din);
+    cudaFree(dout);
+    return res;
+  }
+
+  const void *convert_dev(const double2 *src, i64 n, double scale, i64 L1,
+                          i64 L2) {
+    void *p = dalloc((size_t)n * P_->esz);
+    if (P_->ctype == FM_C64)
+      k_convert<float2><<<grid_for(n), 256>>>((float2 *)p, src, n, scale, L1,
+                                               L2);
+    else
+      k_convert<double2><<<grid_for(n), 256>>>((double2 *)p, src, n, scale,
+                                                L1, L2);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaDeviceSynchronize());
+    // host copy for chunked-step normalisation
+    std::vector<cd> h((size_t)n);
+    std::vector<double2> raw((size_t)n);
+    CUDA_TRY(cudaMemcpy(raw.data(), src, n * sizeof(double2),
+                        cudaMemcpyDeviceToHost));
+    for (i64 o = 0; o < n; ++o) {
+      i64 s = o;
+      if (L1 > 0) s = (o / L2) + L1 * (o % L2);
+      h[o] = cd(raw[s].x, raw[s].y) * scale;
+    }
+    host_vec_[p] = h;
+    return p;
+  }
+
+  // ---------------------------------------------------------- FFT helpers
+  std::vector<int> radices(i64 n) {
+    std::vector<int> r;
+    for (int p : {7, 5, 3})
+      while (n % p == 0) {
+        r.push_back(p);
+        n /= p;
+      }
+    const int big = ept_ >= 16 ? 16 : 8;
+    while (n % big == 0) {
+      r.push_back(big);
+      n /= big;
+    }
+    for (int p : {8, 4, 2})
+      while (n % p == 0) {
+        r.push_back(p);
+        n /= p;
+      }
+    if (n != 1) fail(FM_ERR_UNSUPPORTED, "FFT length is not 2,3,5,7-smooth");
+    return r;
+  }
+
+  fmk::Op fft_op(i64 n, int sign) {
+    if (!cplx_) fail(FM_ERR_TYPE, "Fourier-type operator in a real plan");
+    fmk::Op o = mkop(fmk::OP_FFT, (int)n);
+    o.sign = sign;
+    std::vector<int> r = radices(n);
+    if (r.size() > sizeof(o.rad)) fail(FM_ERR_UNSUPPORTED, "FFT too long");
+    o.nrad = (int)r.size();
+    for (size_t i = 0; i < r.size(); ++i) o.rad[i] = (unsigned char)r[i];
+    o.ptr = twiddle(n);
+    return o;
+  }
+
+  fmk::Op fwht_op(i64 n) {
+    fmk::Op o = mkop(fmk::OP_FWHT, (int)n);
+    int bits = 0;
+    while ((1LL << bits) < n) ++bits;
+    const int g = ept_ >= 16 ? 4 : 3;
+    while (bits > 0) {
+      const int k = std::min(g, bits);
+      o.rad[o.nrad++] = (unsigned char)k;
+      bits -= k;
+    }
+    return o;
+  }
+
+  fmk::Op mul_op(const void *v, i64 len, bool conj) {
+    fmk::Op o = mkop(fmk::OP_MUL, (int)len);
+    o.ptr = v;
+    o.sign = conj ? 1 : 0;
+    return o;
+  }
+
+  fmk::Op zpad_op(i64 from, i64 to) {
+    fmk::Op o = mkop(fmk::OP_ZPAD, (int)from);
+    o.len2 = (int)to;
+    return o;
+  }
+
+  fmk::Op gather_op(const std::vector<i64> &map) {
+    fmk::Op o = mkop(fmk::OP_GATHER, (int)map.size());
+    o.ptr = upload_map(map);
+    return o;
+  }
+
+  // split N = N1 * N2 with both factors <= limit, N1 as close to sqrt(N)
+  void split2(i64 N, i64 limit, i64 &N1, i64 &N2) {
+    N1 = 0;
+    const double r = std::sqrt((double)N);
+    double best = 1e300;
+    for (i64 d = 2; d <= limit && d < N; ++d) {
+      if (N % d) continue;
+      const i64 e = N / d;
+      if (e > limit || !smooth(d) || !smooth(e)) continue;
+      // prefer power-of-two factors and balanced splits
+      const double score = std::fabs(std::log((double)d / r)) +
+                           (is_pow2(d) && is_pow2(e) ? 0 : 0.5);
+      if (score < best) {
+        best = score;
+        N1 = d;
+      }
+    }
+    if (!N1)
+      fail(FM_ERR_UNSUPPORTED,
+           "transform length " + std::to_string(N) +
+               " exceeds the two-pass limit");
+    N2 = N / N1;
+  }
+
+  // ---------------------------------------------------------- units
+  Unit prog(std::vector<fmk::Op> ops, i64 n_in, i64 n_out, i64 L) {
+    Unit u;
+    u.kind = Unit::PROG;
+    u.ops = std::move(ops);
+    u.n_in = n_in;
+    u.n_out = n_out;
+    u.L = L;
+    return u;
+  }
+
+  // circular convolution of length L with a device spectrum (natural
+  // layout for the in-smem program, four-step layout for long L)
+  Chain conv(i64 L, i64 n_in, i64 n_out, const std::vector<cd> &filt,
+             bool conj, const void *pre = nullptr, const void *post = nullptr,
+             bool conj_io = false) {
+    Chain c;
+    const i64 lim = has_odd(L) ? lmax_ / 2 : lmax_;
+    if (L <= lim) {
+      const void *S = spectrum(filt);
+      std::vector<fmk::Op> ops;
+      if (conj_io) ops.push_back(mkop(fmk::OP_CONJ, (int)n_in));
+      if (pre) ops.push_back(mul_op(pre, n_in, false));
+      if (n_in < L) ops.push_back(zpad_op(n_in, L));
+      ops.push_back(fft_op(L, -1));
+      ops.push_back(mul_op(S, L, conj));
+      ops.push_back(fft_op(L, +1));
+      if (post) ops.push_back(mul_op(post, n_out, false));
+      if (conj_io) ops.push_back(mkop(fmk::OP_CONJ, (int)n_out));
+      c.push_back(prog(ops, n_in, n_out, L));
+      return c;
+    }
+    i64 L1, L2;
+    split2(L, has_odd(L) ? lmax_ / 2 : lmax_, L1, L2);
+    const void *S = spectrum(filt, L1, L2);
+    Unit u;
+    u.kind = Unit::STEPS;
+    u.n_in = n_in;
+    u.n_out = n_out;
+    u.tmp_rows.push_back(L);
+    SStep a;
+    a.vin = a.vout = fmk::View{1, L1, L2};
+    a.in_rows = n_in;
+    a.out_rows = L;
+    a.L = a.in_len = a.out_len = (int)L1;
+    a.src = -1;
+    a.dst = 0;
+    a.pre = pre;
+    a.conj_in = conj_io;
+    a.ops.push_back(fft_op(L1, -1));
+    fmk::Op tw = mkop(fmk::OP_TW, (int)L1);
+    tw.ptr = twiddle(L);
+    tw.N = L;
+    tw.sign = -1;
+    tw.div = 1;
+    tw.mod = L2;
+    a.ops.push_back(tw);
+    SStep b;
+    b.vin = b.vout = fmk::View{L1, L2, 1};
+    b.in_rows = b.out_rows = L;
+    b.L = b.in_len = b.out_len = (int)L2;
+    b.src = 0;
+    b.dst = 0;
+    b.ops.push_back(fft_op(L2, -1));
+    fmk::Op m = mul_op(S, L2, conj);
+    m.div = 1;
+    m.mod = L1;
+    m.stride = L2;
+    b.ops.push_back(m);
+    b.ops.push_back(fft_op(L2, +1));
+    fmk::Op tw2 = mkop(fmk::OP_TW, (int)L2);
+    tw2.ptr = twiddle(L);
+    tw2.N = L;
+    tw2.sign = +1;
+    tw2.div = 1;
+    tw2.mod = L1;
+    b.ops.push_back(tw2);
+    SStep cc;
+    cc.vin = cc.vout = fmk::View{1, L1, L2};
+    cc.in_rows = L;
+    cc.out_rows = n_out;
+    cc.L = cc.in_len = cc.out_len = (int)L1;
+    cc.src = 0;
+    cc.dst = -2;
+    cc.post = post;
+    cc.conj_out = conj_io;
+    cc.ops.push_back(fft_op(L1, +1));
+    u.steps = {a, b, cc};
+    c.push_back(u);
+    return c;
+  }
+
+  bool has_odd(i64 L) { return L % 3 == 0 || L % 5 == 0 || L % 7 == 0; }
+
+  Chain fourier(i64 N, bool fwd) {
+    const int sign = fwd ? -1 : +1;
+    Chain c;
+    if (smooth(N)) {
+      const i64 lim = has_odd(N) ? lmax_ / 2 : lmax_;
+      if (N <= lim) {
+        c.push_back(prog({fft_op(N, sign)}, N, N, N));
+        return c;
+      }
+      i64 N1, N2;
+      split2(N, lim, N1, N2);
+      Unit u;
+      u.kind = Unit::STEPS;
+      u.n_in = u.n_out = N;
+      u.tmp_rows.push_back(N);
+      SStep a;
+      a.vin = a.vout = fmk::View{1, N1, N2};
+      a.in_rows = a.out_rows = N;
+      a.L = a.in_len = a.out_len = (int)N1;
+      a.src = -1;
+      a.dst = 0;
+      a.ops.push_back(fft_op(N1, sign));
+      fmk::Op tw = mkop(fmk::OP_TW, (int)N1);
+      tw.ptr = twiddle(N);
+      tw.N = N;
+      tw.sign = sign;
+      tw.div = 1;
+      tw.mod = N2;
+      a.ops.push_back(tw);
+      SStep b;
+      b.vin = fmk::View{N1, N2, 1};
+      b.vout = fmk::View{1, N2, N1};
+      b.in_rows = b.out_rows = N;
+      b.L = b.in_len = b.out_len = (int)N2;
+      b.src = 0;
+      b.dst = -2;
+      b.ops.push_back(fft_op(N2, sign));
+      u.steps = {a, b};
+      c.push_back(u);
+      return c;
+    }
+    // Bluestein: x -> a . x -> (*) h -> a . (first N)
+    const i64 Lb = next_pow2(2 * N - 1);
+    double2 *da = nullptr, *dh = nullptr;
+    CUDA_TRY(cudaMalloc(&da, N * sizeof(double2)));
+    CUDA_TRY(cudaMalloc(&dh, Lb * sizeof(double2)));
+    k_chirp<<<grid_for(N), 256>>>(da, N);
+    k_bluestein_filter<<<grid_for(Lb), 256>>>(dh, da, N, Lb);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaDeviceSynchronize());
+    const void *chirp = convert_dev(da, N, 1.0, 0, 0);
+    std::vector<double2> hh((size_t)Lb);
+    CUDA_TRY(cudaMemcpy(hh.data(), dh, Lb * sizeof(double2),
+                        cudaMemcpyDeviceToHost));
+    cudaFree(da);
+    cudaFree(dh);
+    std::vector<cd> filt((size_t)Lb);
+    for (i64 i = 0; i < Lb; ++i) filt[i] = cd(hh[i].x, hh[i].y);
+    return conv(Lb, N, N, filt, false, chirp, chirp, !fwd);
+  }
+
+  Chain compile(int id, bool fwd) {
+    const NodeRec &r = nodes_[id];
+    const fm_node &d = r.d;
+    const i64 n_in = fwd ? d.cols : d.rows;
+    const i64 n_out = fwd ? d.rows : d.cols;
+    Chain c;
+    switch (d.kind) {
+      case FM_NODE_FOURIER: return fourier(d.n, fwd);
+      case FM_NODE_CIRCULANT: {
+        const i64 n = d.len0;
+        std::vector<cd> cv = node_vec(d, 0);
+        i64 L = n;
+        if (!smooth(n)) L = next_pow2(2 * n - 1);
+        std::vector<cd> filt((size_t)L, cd(0, 0));
+        for (i64 i = 0; i < n; ++i) filt[i] = cv[i];
+        if (L != n)
+          for (i64 i = 1; i < n; ++i) filt[L - n + i] = cv[i];
+        return conv(L, n, n, filt, !fwd);
+      }
+      case FM_NODE_TOEPLITZ: {
+        const i64 nr = d.len0, nc = d.len1 + 1;
+        std::vector<cd> vc = node_vec(d, 0), vr = node_vec(d, 1);
+        const i64 dd = nr + nc - 1;
+        const i64 L = smooth(dd) && is_pow2(dd) ? dd : next_pow2(dd);
+        std::vector<cd> filt((size_t)L, cd(0, 0));
+        for (i64 i = 0; i < nr; ++i) filt[i] = vc[i];
+        for (i64 i = 0; i < nc - 1; ++i) filt[L - (nc - 1) + i] = vr[i];
+        return fwd ? conv(L, nc, nr, filt, false) : conv(L, nr, nc, filt, true);
+      }
+      case FM_NODE_HADAMARD: {
+        const i64 N = 1LL << d.n;
+        if (N <= lmax_) {
+          c.push_back(prog({fwht_op(N)}, N, N, N));
+          return c;
+        }
+        const int p1 = (int)(d.n / 2), p2 = (int)(d.n - p1);
+        const i64 N1 = 1LL << p1, N2 = 1LL << p2;
+        Unit u;
+        u.kind = Unit::STEPS;
+        u.n_in = u.n_out = N;
+        SStep a;
+        a.vin = a.vout = fmk::View{1, N1, N2};
+        a.in_rows = a.out_rows = N;
+        a.L = a.in_len = a.out_len = (int)N1;
+        a.src = -1;
+        a.dst = -2;
+        a.ops.push_back(fwht_op(N1));
+        SStep b;
+        b.vin = b.vout = fmk::View{N1, N2, 1};
+        b.in_rows = b.out_rows = N;
+        b.L = b.in_len = b.out_len = (int)N2;
+        b.src = -2;
+        b.dst = -2;
+        b.ops.push_back(fwht_op(N2));
+        u.steps = {a, b};
+        c.push_back(u);
+        return c;
+      }
+      case FM_NODE_DIAG: {
+        const void *dv = upload(node_vec(d, 0));
+        c.push_back(prog({mul_op(dv, d.len0, !fwd)}, d.len0, d.len0, d.len0));
+        return c;
+      }
+      case FM_NODE_PERMUTATION: {
+        std::vector<i64> s = node_idx(d, 0);
+        const i64 n = (i64)s.size();
+        std::vector<i64> t((size_t)n, -1);
+        for (i64 i = 0; i < n; ++i) {
+          if (s[i] < 0 || s[i] >= n || t[s[i]] >= 0)
+            fail(FM_ERR_VALUE, "Not a permutation.");
+          t[s[i]] = i;
+        }
+        c.push_back(prog({gather_op(fwd ? s : t)}, n, n, n));
+        return c;
+      }
+      case FM_NODE_PARTIAL: {
+        const NodeRec &ch = nodes_[r.ch.at(0)];
+        const i64 crow = ch.d.rows, ccol = ch.d.cols;
+        std::vector<i64> rows, cols;
+        if (d.vec0) rows = node_idx(d, 0);
+        if (d.vec1) cols = node_idx(d, 1);
+        auto check = [](const std::vector<i64> &v, i64 n) {
+          for (i64 x : v)
+            if (x < 0 || x >= n)
+              fail(FM_ERR_VALUE, "Partial: index exceeds matrix dimensions.");
+        };
+        check(rows, crow);
+        check(cols, ccol);
+        auto inverse = [](const std::vector<i64> &sel, i64 n) {
+          std::vector<i64> inv((size_t)n, -1);
+          for (size_t k = 0; k < sel.size(); ++k) inv[sel[k]] = (i64)k;
+          return inv;
+        };
+        const std::vector<i64> &sel_in = fwd ? cols : rows;
+        const std::vector<i64> &sel_out = fwd ? rows : cols;
+        const bool has_in = fwd ? d.vec1 != nullptr : d.vec0 != nullptr;
+        const bool has_out = fwd ? d.vec0 != nullptr : d.vec1 != nullptr;
+        const i64 full_in = fwd ? ccol : crow;
+        if (has_in) {
+          std::vector<i64> inv = inverse(sel_in, full_in);
+          c.push_back(prog({gather_op(inv)}, (i64)sel_in.size(), full_in,
+                           std::max<i64>(full_in, (i64)sel_in.size())));
+        }
+        Chain inner = compile(r.ch.at(0), fwd);
+        c.insert(c.end(), inner.begin(), inner.end());
+        if (has_out) {
+          const i64 full_out = fwd ? crow : ccol;
+          c.push_back(prog({gather_op(sel_out)}, full_out,
+                           (i64)sel_out.size(),
+                           std::max<i64>(full_out, (i64)sel_out.size())));
+        }
+        return c;
+      }
+      case FM_NODE_PRODUCT: {
+        const bool scaled = d.scalar_re != 1.0 || d.scalar_im != 0.0;
+        if (scaled) {
+          fmk::Op s = mkop(fmk::OP_SCALE, (int)n_in);
+          s.sre = d.scalar_re;
+          s.sim = fwd ? d.scalar_im : -d.scalar_im;
+          if (!cplx_ && s.sim != 0.0)
+            fail(FM_ERR_TYPE, "complex scalar in a real plan");
+          c.push_back(prog({s}, n_in, n_in, n_in));
+        }
+        const int k = (int)r.ch.size();
+        for (int i = 0; i < k; ++i) {
+          const int idx = fwd ? r.ch[k - 1 - i] : r.ch[i];
+          Chain t = compile(idx, fwd);
+          c.insert(c.end(), t.begin(), t.end());
+        }
+        return c;
+      }
+      case FM_NODE_SUM: {
+        Unit u;
+        u.kind = Unit::SUM;
+        u.n_in = n_in;
+        u.n_out = n_out;
+        for (int ch : r.ch) u.terms.push_back(compile(ch, fwd));
+        c.push_back(u);
+        return c;
+      }
+      case FM_NODE_KRON: return kron(r, fwd);
+      case FM_NODE_HERMITIAN: return compile(r.ch.at(0), !fwd);
+      case FM_NODE_CONJUGATE: {
+        c.push_back(prog({mkop(fmk::OP_CONJ, (int)n_in)}, n_in, n_in, n_in));
+        Chain t = compile(r.ch.at(0), fwd);
+        c.insert(c.end(), t.begin(), t.end());
+        c.push_back(
+            prog({mkop(fmk::OP_CONJ, (int)n_out)}, n_out, n_out, n_out));
+        return c;
+      }
+      case FM_NODE_EYE: return c;
+      case FM_NODE_DENSE: {
+        const i64 R = d.rows, C = d.cols;
+        std::vector<cd> a = node_vec(d, 0);
+        if ((i64)a.size() != R * C) fail(FM_ERR_VALUE, "dense data size");
+        std::vector<cd> m((size_t)(R * C));
+        if (fwd) m = a;
+        else
+          for (i64 i = 0; i < R; ++i)
+            for (i64 j = 0; j < C; ++j) m[j + i * C] = std::conj(a[i + j * R]);
+        fmk::Op o = mkop(fmk::OP_DENSE, (int)n_out);
+        o.len2 = (int)n_in;
+        o.ptr = upload(m);
+        c.push_back(prog({o}, n_in, n_out, std::max(n_in, n_out)));
+        return c;
+      }
+      default: fail(FM_ERR_UNSUPPORTED, "unknown node kind");
+    }
+  }
+
+  // merge consecutive PROG units of a chain (when the result fits)
+  Chain merged(const Chain &in) {
+    Chain out;
+    for (const Unit &u : in) {
+      if (u.kind == Unit::PROG && !out.empty() &&
+          out.back().kind == Unit::PROG) {
+        Unit &p = out.back();
+        const i64 L = std::max(p.L, u.L);
+        std::vector<fmk::Op> cat = p.ops;
+        cat.insert(cat.end(), u.ops.begin(), u.ops.end());
+        if (L <= limit_for(cat) && cat.size() <= (size_t)FM_MAX_OPS) {
+          p.ops.insert(p.ops.end(), u.ops.begin(), u.ops.end());
+          p.n_out = u.n_out;
+          p.L = L;
+          continue;
+        }
+      }
+      out.push_back(u);
+    }
+    return out;
+  }
+
+  Chain kron(const NodeRec &r, bool fwd) {
+    std::vector<i64> dims;
+    for (int ch : r.ch) dims.push_back(nodes_[ch].d.rows);
+    i64 N = 1;
+    for (i64 x : dims) N *= x;
+    Unit u;
+    u.kind = Unit::STEPS;
+    u.n_in = u.n_out = N;
+    const int K = (int)dims.size();
+    // apply the contiguous (last) mode first, then outward
+    for (int step = 0; step < K; ++step) {
+      const int k = K - 1 - step;
+      Chain fc = merged(compile(r.ch[k], fwd));
+      if (fc.empty()) continue;  // identity factor
+      if (fc.size() != 1 || fc[0].kind != Unit::PROG)
+        fail(FM_ERR_UNSUPPORTED,
+             "Kron factor too large for a single shared-memory program");
+      const Unit &p = fc[0];
+      if (p.L > limit_for(p.ops))
+        fail(FM_ERR_UNSUPPORTED, "Kron factor too large");
+      i64 A = 1, Cc = 1;
+      for (int i = 0; i < k; ++i) A *= dims[i];
+      for (int i = k + 1; i < K; ++i) Cc *= dims[i];
+      SStep s;
+      s.vin = s.vout = fmk::View{A, dims[k], Cc};
+      s.in_rows = s.out_rows = N;
+      s.L = (int)p.L;
+      s.in_len = s.out_len = (int)dims[k];
+      s.ops = p.ops;
+      s.src = u.steps.empty() ? -1 : -2;
+      s.dst = -2;
+      u.steps.push_back(s);
+    }
+    Chain c;
+    if (!u.steps.empty()) c.push_back(u);
+    return c;
+  }
+
+  // ---------------------------------------------------------- lowering
+  int new_scratch(i64 rows) {
+    P_->scratch_rows.push_back(rows);
+    return 1 + (int)P_->scratch_rows.size();
+  }
+
+  int kernel_class(const std::vector<fmk::Op> &ops) {
+    bool fft = false, odd = false, fwht = false, gen = false;
+    for (const fmk::Op &o : ops) {
+      if (o.kind == fmk::OP_FFT) {
+        fft = true;
+        for (int i = 0; i < o.nrad; ++i)
+          if (o.rad[i] & 1) odd = true;
+      }
+      if (o.kind == fmk::OP_FWHT) fwht = true;
+      if (o.kind == fmk::OP_GATHER || o.kind == fmk::OP_DENSE) gen = true;
+    }
+    if (gen || (fft && fwht)) return 0;
+    if (fwht) return 3;
+    if (fft) return odd ? 2 : 1;
+    return 3;
+  }
+
+  // longest working length a program of this op mix may use in one tile
+  i64 limit_for(const std::vector<fmk::Op> &ops) {
+    const int cls = kernel_class(ops);
+    return (cls == 0 || cls == 2) ? lmax_ / 2 : lmax_;
+  }
+
+  void finish(LStep &ls, const std::vector<fmk::Op> &ops) {
+    fmk::Step &st = ls.st;
+    if ((int)ops.size() > FM_MAX_OPS)
+      fail(FM_ERR_UNSUPPORTED, "operator chain too long for one launch");
+    st.nops = (int)ops.size();
+    for (size_t i = 0; i < ops.size(); ++i) st.ops[i] = ops[i];
+    ls.cls = kernel_class(ops);
+    bool odd = ls.cls == 2 || ls.cls == 0;
+    const int ept = odd ? ept_ / 2 : ept_;
+    const int L = std::max(st.L, 1);
+    int Lp = fmk::pidx<float2>(0);  // placeholder, recomputed below
+    const int shift = P_->esz >= 16 ? 3 : (P_->esz == 8 ? 4 : 5);
+    Lp = (L - 1) + ((L - 1) >> shift) + 1;
+    if ((Lp & 1) == 0) ++Lp;
+    st.Lp = Lp;
+    const i64 nvec = st.V;  // per column; tiles may span columns
+    const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
+    int B = 1;
+    if (strided) {
+      const int coal = std::max(1, 128 / P_->esz);
+      B = coal;
+    }
+    auto threads_for = [&](int b) {
+      i64 t = ((i64)b * L + ept - 1) / ept;
+      t = (t + 31) / 32 * 32;
+      return (int)std::max<i64>(t, 32);
+    };
+    const size_t budget = 96 * 1024;
+    while (B > 1 && (threads_for(B) > FM_MAX_THREADS ||
+                     (size_t)B * Lp * P_->esz > (size_t)fmk::kMaxSmem))
+      B /= 2;
+    while (threads_for(B) < 128 && threads_for(2 * B) <= FM_MAX_THREADS &&
+           (size_t)2 * B * Lp * P_->esz <= budget &&
+           (i64)B < nvec * 64)
+      B *= 2;
+    if (threads_for(B) > FM_MAX_THREADS)
+      fail(FM_ERR_UNSUPPORTED, "working length too large for one tile");
+    st.B = B;
+    ls.threads = threads_for(B);
+    ls.smem = (size_t)B * Lp * P_->esz;
+    if (ls.smem > (size_t)fmk::kMaxSmem)
+      fail(FM_ERR_UNSUPPORTED, "tile exceeds shared memory");
+  }
+
+  fmk::Step base_step() {
+    fmk::Step st;
+    memset(&st, 0, sizeof(st));
+    st.scale_re = 1.0;
+    return st;
+  }
+
+  void emit_copy(int src, int dst, i64 n, std::vector<LStep> &out) {
+    Unit u = prog({}, n, n, n);
+    emit_prog(u, src, dst, out);
+  }
+
+  // whole-column program, or a chunked pointwise/gather program
+  void emit_prog(const Unit &u, int src, int dst, std::vector<LStep> &out) {
+    if (u.L <= limit_for(u.ops)) {
+      LStep ls;
+      ls.src = src;
+      ls.dst = dst;
+      fmk::Step &st = ls.st;
+      st = base_step();
+      st.vin = fmk::View{1, u.n_in, 1};
+      st.vout = fmk::View{1, u.n_out, 1};
+      st.in_rows = u.n_in;
+      st.out_rows = u.n_out;
+      st.in_len = (int)u.n_in;
+      st.out_len = (int)u.n_out;
+      st.L = (int)std::max<i64>(u.L, 1);
+      st.V = 1;
+      finish(ls, u.ops);
+      out.push_back(ls);
+      return;
+    }
+    emit_chunked(u, src, dst, out);
+  }
+
+  // y[i] = s * d[i] * cx(x[map[i]]) over chunks of the column
+  void emit_chunked(const Unit &u, int src, int dst, std::vector<LStep> &out) {
+    i64 len = u.n_in;
+    std::vector<i64> map;  // empty: identity
+    std::vector<cd> dv;    // empty: ones
+    cd s(1, 0);
+    bool cx = false;
+    for (const fmk::Op &o : u.ops) {
+      switch (o.kind) {
+        case fmk::OP_GATHER: {
+          const std::vector<i64> &m = host_map_.at(o.ptr);
+          std::vector<i64> nm(m.size());
+          std::vector<cd> nd;
+          if (!dv.empty()) nd.resize(m.size());
+          for (size_t i = 0; i < m.size(); ++i) {
+            const i64 j = m[i];
+            nm[i] = j < 0 ? -1 : (map.empty() ? j : map[j]);
+            if (!dv.empty()) nd[i] = j < 0 ? cd(0, 0) : dv[j];
+          }
+          map.swap(nm);
+          if (!dv.empty()) dv.swap(nd);
+          len = (i64)m.size();
+          break;
+        }
+        case fmk::OP_MUL: {
+          const std::vector<cd> &v = host_vec_.at(o.ptr);
+          if (dv.empty()) dv.assign((size_t)len, cd(1, 0));
+          for (i64 i = 0; i < len; ++i)
+            dv[i] *= o.sign ? std::conj(v[i]) : v[i];
+          break;
+        }
+        case fmk::OP_SCALE: s *= cd(o.sre, o.sim); break;
+        case fmk::OP_CONJ:
+          s = std::conj(s);
+          for (cd &x : dv) x = std::conj(x);
+          cx = !cx;
+          break;
+        default:
+          fail(FM_ERR_UNSUPPORTED,
+               "long vector program with non-pointwise operations");
+      }
+    }
+    const i64 n_out = len;
+    const i64 Lc = std::min<i64>(2048, std::max<i64>(n_out, 1));
+    const i64 nch = (n_out + Lc - 1) / Lc;
+    LStep ls;
+    ls.src = src;
+    ls.dst = dst;
+    fmk::Step &st = ls.st;
+    st = base_step();
+    st.vin = st.vout = fmk::View{nch, Lc, 1};
+    st.in_rows = map.empty() ? u.n_in : n_out;
+    st.out_rows = n_out;
+    st.in_len = st.out_len = (int)Lc;
+    st.L = (int)Lc;
+    st.V = nch;
+    if (!map.empty()) st.map_in = upload_map(map);
+    st.conj_in = cx;
+    std::vector<fmk::Op> ops;
+    if (!dv.empty()) {
+      dv.resize((size_t)(nch * Lc), cd(0, 0));
+      fmk::Op m = mul_op(upload(dv), Lc, false);
+      m.div = 1;
+      m.mod = nch;
+      m.stride = Lc;
+      ops.push_back(m);
+    }
+    if (s != cd(1, 0)) {
+      st.has_scale = 1;
+      st.scale_re = s.real();
+      st.scale_im = s.imag();
+    }
+    finish(ls, ops);
+    out.push_back(ls);
+  }
+
+  void emit_steps(const Unit &u, int src, int dst, std::vector<LStep> &out) {
+    std::vector<int> tmp;
+    for (i64 rows : u.tmp_rows) tmp.push_back(new_scratch(rows));
+    auto resolve = [&](int id) {
+      if (id == -1) return src;
+      if (id == -2) return dst;
+      return tmp.at(id);
+    };
+    for (const SStep &s : u.steps) {
+      LStep ls;
+      ls.src = resolve(s.src);
+      ls.dst = resolve(s.dst);
+      fmk::Step &st = ls.st;
+      st = base_step();
+      st.vin = s.vin;
+      st.vout = s.vout;
+      st.in_rows = s.in_rows;
+      st.out_rows = s.out_rows;
+      st.in_len = s.in_len;
+      st.out_len = s.out_len;
+      st.L = s.L;
+      st.V = s.vin.A * s.vin.Cc;
+      st.pre = s.pre;
+      st.post = s.post;
+      st.conj_in = s.conj_in;
+      st.conj_out = s.conj_out;
+      finish(ls, s.ops);
+      out.push_back(ls);
+    }
+  }
+
+  void lower(const Chain &chain_in, int in_id, i64 in_rows, int out_id,
+             i64 out_rows, std::vector<LStep> &out) {
+    const Chain chain = merged(chain_in);
+    if (chain.empty()) {
+      emit_copy(in_id, out_id, in_rows, out);
+      return;
+    }
+    int cur = in_id;
+    for (size_t i = 0; i < chain.size(); ++i) {
+      const Unit &u = chain[i];
+      const bool last = i + 1 == chain.size();
+      const int dst = last ? out_id : new_scratch(u.n_out);
+      switch (u.kind) {
+        case Unit::PROG: emit_prog(u, cur, dst, out); break;
+        case Unit::STEPS: emit_steps(u, cur, dst, out); break;
+        case Unit::SUM: {
+          for (size_t t = 0; t < u.terms.size(); ++t) {
+            if (t == 0) {
+              lower(u.terms[t], cur, u.n_in, dst, u.n_out, out);
+              continue;
+            }
+            // later terms: evaluate into scratch, then accumulate
+            const int tmp = new_scratch(u.n_out);
+            lower(u.terms[t], cur, u.n_in, tmp, u.n_out, out);
+            Unit cp = prog({}, u.n_out, u.n_out, u.n_out);
+            std::vector<LStep> acc;
+            emit_prog(cp, tmp, dst, acc);
+            for (LStep &a : acc) a.st.accumulate = 1;
+            out.insert(out.end(), acc.begin(), acc.end());
+          }
+          break;
+        }
+      }
+      cur = dst;
+    }
+    (void)out_rows;
+  }
+};
+
+// ------------------------------------------------------------ execution
+int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
+             void *y, int y_type, i64 ld_y, i64 M, cudaStream_t s,
+             std::vector<cudaEvent_t> *events) {
+  if (M <= 0) return FM_OK;
+  // scratch
+  const size_t align = 256;
+  std::vector<size_t> offs(P->scratch_rows.size());
+  size_t total = 0;
+  for (size_t k = 0; k < P->scratch_rows.size(); ++k) {
+    offs[k] = total;
+    total += ((size_t)P->scratch_rows[k] * M * P->esz + align - 1) / align *
+             align;
+  }
+  if (total > P->scratch_cap) {
+    if (P->scratch) {
+      cudaStreamSynchronize(s);
+      cudaFree(P->scratch);
+      P->scratch = nullptr;
+      P->scratch_cap = 0;
+    }
+    CUDA_TRY(cudaMalloc(&P->scratch, total));
+    P->scratch_cap = total;
+  }
+  size_t li = 0;
+  if (events) CUDA_TRY(cudaEventRecord((*events)[li++], s));
+  for (const LStep &ls : P->steps[dir]) {
+    fmk::Step st = ls.st;
+    auto bind = [&](int id, const void *&ptr, int &type, i64 &ld) {
+      if (id == 0) {
+        ptr = x;
+        type = x_type;
+        ld = ld_x;
+      } else if (id == 1) {
+        ptr = y;
+        type = y_type;
+        ld = ld_y;
+      } else {
+        ptr = (char *)P->scratch + offs[id - 2];
+        type = P->ctype;
+        ld = P->scratch_rows[id - 2];
+      }
+    };
+    const void *sp;
+    const void *dp;
+    bind(ls.src, sp, st.src_type, st.ld_src);
+    bind(ls.dst, dp, st.dst_type, st.ld_dst);
+    st.src = sp;
+    st.dst = const_cast<void *>(dp);
+    st.num_cols = M;
+    const i64 grid = (st.V * M + st.B - 1) / st.B;
+    if (grid > 0x7fffffffLL) fail(FM_ERR_VALUE, "too many columns");
+    cudaError_t e;
+    switch (P->ctype) {
+      case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      default: e = fmk::launch_c128(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+    }
+    CUDA_TRY(e);
+    if (events) CUDA_TRY(cudaEventRecord((*events)[li++], s));
+  }
+  return FM_OK;
+}
+
+const char *kind_name(int k) {
+  switch (k) {
+    case fmk::OP_FFT: return "fft";
+    case fmk::OP_MUL: return "mul";
+    case fmk::OP_ZPAD: return "zpad";
+    case fmk::OP_GATHER: return "gather";
+    case fmk::OP_FWHT: return "fwht";
+    case fmk::OP_DENSE: return "dense";
+    case fmk::OP_SCALE: return "scale";
+    case fmk::OP_CONJ: return "conj";
+    case fmk::OP_TW: return "twiddle";
+  }
+  return "?";
+}
+
+template <class F> int guarded(F f) {
+  try {
+    g_err.clear();
+    return f();
+  } catch (const Error &e) {
+    g_err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_err = "host allocation failed";
+    return FM_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return FM_ERR_VALUE;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ C ABI
+extern "C" {
+
+int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
+                   const int32_t *children, int32_t num_children, int32_t root,
+                   int32_t compute_type, fm_plan **out_plan) {
+  return guarded([&]() {
+    if (!out_plan) fail(FM_ERR_VALUE, "out_plan is NULL");
+    *out_plan = nullptr;
+    if (!nodes || num_nodes <= 0 || root < 0 || root >= num_nodes)
+      fail(FM_ERR_VALUE, "invalid node array");
+    if (compute_type != FM_F32 && compute_type != FM_F64 &&
+        compute_type != FM_C64 && compute_type != FM_C128 &&
+        compute_type != FM_I64)
+      fail(FM_ERR_TYPE, "unsupported compute type");
+    std::vector<NodeRec> recs((size_t)num_nodes);
+    for (int i = 0; i < num_nodes; ++i) {
+      recs[i].d = nodes[i];
+      const fm_node &d = nodes[i];
+      if (d.num_children < 0 ||
+          (d.num_children > 0 &&
+           (!children || d.first_child < 0 ||
+            d.first_child + d.num_children > num_children)))
+        fail(FM_ERR_VALUE, "invalid child range");
+      for (int k = 0; k < d.num_children; ++k) {
+        const int c = children[d.first_child + k];
+        if (c < 0 || c >= num_nodes) fail(FM_ERR_VALUE, "invalid child");
+        recs[i].ch.push_back(c);
+      }
+      if (d.rows < 0 || d.cols < 0) fail(FM_ERR_VALUE, "negative shape");
+    }
+    std::unique_ptr<fm_plan> P(new fm_plan);
+    P->ctype = compute_type;
+    P->esz = esize(compute_type);
+    CUDA_TRY(cudaGetDevice(&P->device));
+    P->rows = nodes[root].rows;
+    P->cols = nodes[root].cols;
+    Planner(P.get(), recs).build(root);
+    CUDA_TRY(cudaDeviceSynchronize());
+    *out_plan = P.release();
+    return FM_OK;
+  });
+}
+
+int fm_execute(fm_plan *plan, int32_t direction, const void *x, int32_t x_type,
+               int64_t ld_x, void *y, int32_t y_type, int64_t ld_y,
+               int64_t num_cols, void *stream) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    if (!valid_type(x_type) || !valid_type(y_type))
+      fail(FM_ERR_TYPE, "unsupported element type");
+    const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
+    const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
+    if (num_cols < 0) fail(FM_ERR_VALUE, "negative column count");
+    if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "NULL data pointer");
+    if (ld_x < n_in || ld_y < n_out)
+      fail(FM_ERR_VALUE, "leading dimension smaller than the vector size");
+    return run_plan(plan, direction, x, x_type, ld_x, y, y_type, ld_y,
+                    num_cols, (cudaStream_t)stream);
+  });
+}
+
+int fm_execute_profiled(fm_plan *plan, int32_t direction, const void *x,
+                        int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
+                        int64_t ld_y, int64_t num_cols, void *stream,
+                        float *ms, int32_t *num_launches) {
+  return guarded([&]() {
+    if (!plan || !ms || !num_launches) fail(FM_ERR_VALUE, "NULL argument");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    if (!valid_type(x_type) || !valid_type(y_type))
+      fail(FM_ERR_TYPE, "unsupported element type");
+    const size_t n = plan->steps[direction].size();
+    if ((size_t)*num_launches < n) fail(FM_ERR_VALUE, "ms array too short");
+    std::vector<cudaEvent_t> ev(n + 1, nullptr);
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    const cudaStream_t s = (cudaStream_t)stream;
+    int st = FM_OK;
+    try {
+      st = run_plan(plan, direction, x, x_type, ld_x, y, y_type, ld_y,
+                    num_cols, s, &ev);
+      if (st == FM_OK) {
+        CUDA_TRY(cudaEventSynchronize(ev[n]));
+        for (size_t i = 0; i < n; ++i)
+          CUDA_TRY(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+        *num_launches = (int32_t)n;
+      }
+    } catch (...) {
+      for (auto &e : ev) cudaEventDestroy(e);
+      throw;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return st;
+  });
+}
+
+int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
+                    int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
+                    int64_t ld_y, int64_t num_cols) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (!valid_type(x_type) || !valid_type(y_type))
+      fail(FM_ERR_TYPE, "unsupported element type");
+    if (num_cols <= 0) return FM_OK;
+    const size_t bx = (size_t)ld_x * num_cols * esize(x_type);
+    const size_t by = (size_t)ld_y * num_cols * esize(y_type);
+    if (!plan->hstream)
+      CUDA_TRY(cudaStreamCreateWithFlags(&plan->hstream,
+                                         cudaStreamNonBlocking));
+    if (bx > plan->dx_cap) {
+      if (plan->dx) cudaFree(plan->dx);
+      plan->dx = nullptr;
+      plan->dx_cap = 0;
+      CUDA_TRY(cudaMalloc(&plan->dx, bx));
+      plan->dx_cap = bx;
+    }
+    if (by > plan->dy_cap) {
+      if (plan->dy) cudaFree(plan->dy);
+      plan->dy = nullptr;
+      plan->dy_cap = 0;
+      CUDA_TRY(cudaMalloc(&plan->dy, by));
+      plan->dy_cap = by;
+    }
+    CUDA_TRY(cudaMemcpyAsync(plan->dx, x, bx, cudaMemcpyHostToDevice,
+                             plan->hstream));
+    const int st = fm_execute(plan, direction, plan->dx, x_type, ld_x,
+                              plan->dy, y_type, ld_y, num_cols,
+                              plan->hstream);
+    if (st != FM_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(y, plan->dy, by, cudaMemcpyDeviceToHost,
+                             plan->hstream));
+    CUDA_TRY(cudaStreamSynchronize(plan->hstream));
+    return FM_OK;
+  });
+}
+
+int fm_plan_destroy(fm_plan *plan) {
+  return guarded([&]() {
+    delete plan;
+    return FM_OK;
+  });
+}
+
+int fm_plan_get_info(const fm_plan *plan, fm_plan_info *info) {
+  return guarded([&]() {
+    if (!plan || !info) fail(FM_ERR_VALUE, "NULL argument");
+    memset(info, 0, sizeof(*info));
+    info->rows = plan->rows;
+    info->cols = plan->cols;
+    info->num_launches_fwd = (int32_t)plan->steps[0].size();
+    info->num_launches_bwd = (int32_t)plan->steps[1].size();
+    i64 sc = 0;
+    for (i64 r : plan->scratch_rows) sc += r * plan->esz;
+    info->scratch_bytes_per_col = sc;
+    info->const_bytes = plan->const_bytes;
+    info->compute_type = plan->ctype;
+    return FM_OK;
+  });
+}
+
+int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
+                     int64_t buf_len) {
+  return guarded([&]() {
+    if (!plan || !buf || buf_len <= 0) fail(FM_ERR_VALUE, "NULL argument");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    std::string s;
+    char line[512];
+    for (const LStep &ls : plan->steps[direction]) {
+      const fmk::Step &st = ls.st;
+      snprintf(line, sizeof(line),
+               "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,%lld) "
+               "L=%d B=%d threads=%d smem=%zu cls=%d acc=%d:",
+               ls.src, ls.dst, st.vin.A, st.vin.n, st.vin.Cc, st.vout.A,
+               st.vout.n, st.vout.Cc, st.L, st.B, ls.threads, ls.smem, ls.cls,
+               st.accumulate);
+      s += line;
+      for (int i = 0; i < st.nops; ++i) {
+        snprintf(line, sizeof(line), " %s(%d)", kind_name(st.ops[i].kind),
+                 st.ops[i].len);
+        s += line;
+      }
+      if (st.map_in) s += " map_in";
+      if (st.pre) s += " pre";
+      if (st.post) s += " post";
+      s += "\n";
+    }
+    const size_t n = std::min<size_t>(s.size(), (size_t)buf_len - 1);
+    memcpy(buf, s.data(), n);
+    buf[n] = 0;
+    return FM_OK;
+  });
+}
+
+const char *fm_last_error(void) { return g_err.c_str(); }
+
+int32_t fm_version(void) { return 100; }
+
+}  // extern "C"

@@ -1,0 +1,491 @@
+"""The structured operator classes, with fastmat's constructors.
+
+Each class keeps fastmat's constructor signature, dtype rule and the
+attributes callers read, and describes itself to the native engine as one
+node of an operator tree (``_emit``).  ``_reference`` builds the dense
+matrix directly from the defining data, as fastmat's ``.reference()`` does.
+"""
+
+import numpy as np
+
+from . import _native
+from . import fftsize
+from . import types as T
+from .matrix import Hermitian, Matrix
+
+
+def _squeezed_copy(a):
+    a = np.array(a)
+    return np.squeeze(a).copy() if a.ndim > 1 else a.copy()
+
+
+class Fourier(Matrix):
+    """Unnormalised DFT matrix F[n, k] = exp(-2 pi i n k / N)
+    (fastmat/Fourier.pyx:26-285).  ``_numL`` is fastmat's Bluestein length
+    decision (0 = direct); the GPU picks its own algorithm for every order.
+    """
+
+    def __init__(self, order, **options):
+        if order < 1:
+            raise ValueError("Fourier order cannot be smaller than 1.")
+        self._order = int(order)
+        self._numL = fftsize.bluestein_length(
+            self._order, options.get('optimize', True),
+            options.get('maxStage', 4))
+        self._init_properties(self._order, self._order, np.complex128,
+                              **options)
+
+    @property
+    def order(self):
+        return self._order
+
+    def _emit(self, b):
+        return b.add(_native.NODE_FOURIER, self, n=self._order)
+
+    def _reference(self):
+        k = np.arange(self._order, dtype=np.int64)
+        ph = np.outer(k, k) % self._order
+        return np.exp(ph * (-2j * np.pi / self._order)).astype(self.dtype)
+
+
+class Diag(Matrix):
+    """Diagonal matrix (fastmat/Diag.pyx:29-174)."""
+
+    def __init__(self, vecD, **options):
+        self._vecD = _squeezed_copy(vecD)
+        if np.ndim(vecD) != 1 or self._vecD.ndim != 1:
+            raise ValueError(
+                "Diag: Definition vector must have exactly one dimension.")
+        self._vecD = self._vecD.astype(T.supported(self._vecD.dtype),
+                                       copy=False)
+        n = self._vecD.size
+        self._init_properties(n, n, self._vecD.dtype.type, **options)
+
+    @property
+    def vecD(self):
+        return self._vecD
+
+    def _emit(self, b):
+        return b.add(_native.NODE_DIAG, self, vec0=self._vecD)
+
+    def _reference(self):
+        return np.diag(self._vecD)
+
+
+class Eye(Matrix):
+    """Identity (fastmat/Eye.pyx)."""
+
+    def __init__(self, order, **options):
+        self._init_properties(order, order, np.int8, **options)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_EYE, self)
+
+    def _reference(self):
+        return np.eye(self.numRows, dtype=self.dtype)
+
+
+class Hadamard(Matrix):
+    """Sylvester-ordered Hadamard matrix of size 2^order, int8
+    (fastmat/Hadamard.pyx:63-248)."""
+
+    def __init__(self, order, **options):
+        if order < 1:
+            raise ValueError("Hadamard: Order must be larger than 0.")
+        max_order = 62
+        if order > max_order:
+            raise ValueError(
+                "Hadamard: Order exceeds maximum for this platform: %d" %
+                max_order)
+        self._order = int(order)
+        n = 2 ** self._order
+        self._init_properties(n, n, np.int8, **options)
+
+    @property
+    def order(self):
+        return self._order
+
+    def _emit(self, b):
+        return b.add(_native.NODE_HADAMARD, self, n=self._order)
+
+    def _reference(self):
+        h = np.ones((1, 1), dtype=np.int8)
+        for _ in range(self._order):
+            h = np.block([[h, h], [h, -h]])
+        return h
+
+
+class Permutation(Matrix):
+    """Permutation matrix, forward x[sigma] (fastmat/Permutation.pyx)."""
+
+    def __init__(self, sigma, **options):
+        sigma = np.array(sigma)
+        self._sigma = _squeezed_copy(sigma)
+        if sigma.ndim != 1 or self._sigma.ndim != 1:
+            raise ValueError(
+                "Diag: Definition vector must have exactly one dimension.")
+        n = sigma.shape[0]
+        if not np.array_equal(np.sort(sigma), np.arange(n)):
+            raise ValueError("Not a permutation.")
+        self._tau = np.argsort(sigma)
+        self._init_properties(n, n, np.int8, **options)
+
+    @property
+    def sigma(self):
+        return self._sigma
+
+    @property
+    def tau(self):
+        return self._tau
+
+    def _emit(self, b):
+        return b.add(_native.NODE_PERMUTATION, self, vec0=self._sigma,
+                     int0=True)
+
+    def _reference(self):
+        return np.eye(self.numRows, dtype=self.dtype)[self._sigma, :]
+
+
+class Partial(Matrix):
+    """Row/column sub-selection of a matrix (fastmat/Partial.pyx:25-303)."""
+
+    def __init__(self, mat, **options):
+        if not isinstance(mat, Matrix):
+            raise TypeError("Partial: fastmat Matrix required.")
+        self._content = (mat,)
+        if 'N' in options:
+            options['rows'] = options['N']
+        if 'M' in options:
+            options['cols'] = options['M']
+
+        def check(sel, size, name):
+            if sel is None:
+                return None
+            sel = np.array(sel)
+            if sel.dtype == bool:
+                sel = np.arange(size)[sel]
+            elif sel.dtype.kind not in 'iu':
+                raise TypeError(
+                    "Partial: Type of %s indices must be int or bool." % name)
+            if np.any((sel >= size) | (sel < 0)):
+                raise ValueError(
+                    "Partial: A %s index exceeds matrix dimensions." % name)
+            return sel
+
+        self._rowSelection = check(options.pop('rows', None), mat.numRows,
+                                   'row')
+        self._colSelection = check(options.pop('cols', None), mat.numCols,
+                                   'col')
+        options.pop('N', None)
+        options.pop('M', None)
+        self._init_properties(
+            mat.numRows if self._rowSelection is None
+            else len(self._rowSelection),
+            mat.numCols if self._colSelection is None
+            else len(self._colSelection),
+            mat.dtype, **options)
+
+    @property
+    def rowSelection(self):
+        return (self._rowSelection if self._rowSelection is not None
+                else np.arange(self.numRows))
+
+    @property
+    def colSelection(self):
+        return (self._colSelection if self._colSelection is not None
+                else np.arange(self.numCols))
+
+    def _emit(self, b):
+        return b.add(_native.NODE_PARTIAL, self, children=self._content,
+                     vec0=self._rowSelection, vec1=self._colSelection,
+                     int0=True, int1=True)
+
+    def _reference(self):
+        a = self._content[0].reference()
+        if self._rowSelection is not None:
+            a = a[self._rowSelection, :]
+        if self._colSelection is not None:
+            a = a[:, self._colSelection]
+        return a
+
+
+class Product(Matrix):
+    """Matrix product with an optional scalar (fastmat/Product.pyx)."""
+
+    def __init__(self, *matrices, **options):
+        factors = []
+        scalar = np.int8(1)
+        dtype = [np.int8]
+
+        def add(items):
+            nonlocal scalar
+            for f in items:
+                if np.isscalar(f):
+                    dtype[0] = T.promote(dtype[0], np.array(f).dtype)
+                    scalar = np.inner(scalar, f)
+                    continue
+                if not isinstance(f, Matrix):
+                    raise TypeError("Product: Term not scalar nor Matrix.")
+                if isinstance(f, Product):
+                    if f._scalar != 1:
+                        scalar = scalar * f._scalar
+                    add(f.content)
+                else:
+                    factors.append(f)
+                dtype[0] = T.promote(dtype[0], f.dtype)
+
+        add(matrices)
+        dt = dtype[0]
+        expansion = options.pop('typeExpansion', T.safe_type_expansion(dt))
+        if expansion is not None:
+            dt = T.promote(dt, expansion)
+        if not factors:
+            raise ValueError("Product has no terms.")
+        for i in range(1, len(factors)):
+            if factors[i].numRows != factors[i - 1].numCols:
+                raise ValueError(
+                    "Product: Dimension mismatch for term %d [%dx%d]" % (
+                        i, factors[0].numRows, factors[i - 1].numCols))
+        self._scalar = np.array(scalar).astype(dt)
+        self._content = tuple(factors)
+        self._init_properties(factors[0].numRows, factors[-1].numCols, dt,
+                              **options)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_PRODUCT, self, children=self._content,
+                     scalar=complex(self._scalar))
+
+    def _reference(self):
+        dt = T.promote(np.float64, self.dtype)
+        a = np.inner(self._content[-1].reference(), self._scalar.astype(dt))
+        for term in reversed(self._content[:-1]):
+            a = term.reference().dot(a)
+        return a
+
+
+class Sum(Matrix):
+    """Sum of matrices (fastmat/Sum.pyx)."""
+
+    def __init__(self, *matrices, **options):
+        terms = []
+
+        def add(items):
+            for m in items:
+                if not isinstance(m, Matrix):
+                    raise TypeError("Sum: Term is not a fastmat Matrix.")
+                if isinstance(m, Sum):
+                    add(m.content)
+                else:
+                    terms.append(m)
+
+        add(matrices)
+        if not terms:
+            raise ValueError("Sum: No terms given.")
+        for m in terms[1:]:
+            if m.shape != terms[0].shape:
+                raise ValueError("Sum: Term dimension mismatch: " + repr(m))
+        dt = np.int8
+        for m in terms:
+            dt = T.promote(dt, m.dtype)
+        self._content = tuple(terms)
+        options.setdefault('widenInputDatatype', True)
+        self._init_properties(terms[0].numRows, terms[0].numCols, dt,
+                              **options)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_SUM, self, children=self._content)
+
+    def _reference(self):
+        a = np.zeros(self.shape, dtype=self.dtype)
+        for m in self._content:
+            a = a + m.reference()
+        return a
+
+
+class Kron(Matrix):
+    """Kronecker product, factor 0 most significant (fastmat/Kron.pyx)."""
+
+    def __init__(self, *matrices, **options):
+        if len(matrices) < 2:
+            raise ValueError("Kronecker: Product must have at least two terms")
+        dt = np.int8
+        n = 1
+        for m in matrices:
+            if m.numRows != m.numCols:
+                raise ValueError("Kronecker: Product terms must be symmetric")
+            n *= m.numRows
+            dt = T.promote(dt, m.dtype)
+        expansion = options.pop('typeExpansion', T.safe_type_expansion(dt))
+        if expansion is not None:
+            dt = T.promote(dt, expansion)
+        self._content = tuple(matrices)
+        self._dims = tuple(m.numRows for m in matrices)
+        options.setdefault('widenInputDatatype', True)
+        self._init_properties(n, n, dt, **options)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_KRON, self, children=self._content)
+
+    def _reference(self):
+        a = self._content[0].reference().astype(
+            T.promote(self.dtype, np.float64))
+        for m in self._content[1:]:
+            a = np.kron(a, m.reference())
+        return a
+
+
+class Circulant(Partial):
+    """Circulant matrix C[i, j] = c[(i - j) mod n]
+    (fastmat/Circulant.pyx:32-227).  The GPU convolves with the FFT of the
+    defining vector; ``content`` builds fastmat's Fourier-domain structure
+    (Partial of Product(F.H, Diag(fft(c)/L), F)) on demand."""
+
+    def __init__(self, tenC, **options):
+        c = _squeezed_copy(tenC)
+        if np.ndim(tenC) < 1 or c.ndim < 1:
+            raise ValueError("Column-definition tensor must be at least 1D.")
+        if c.ndim > 1:
+            raise NotImplementedError(
+                "multi-level Circulant is not supported by fastmat_gb300")
+        self._optimize = options.get('optimize', True)
+        self._maxStage = options.get('maxStage', 4)
+        self._tenC = c.astype(np.complex128)
+        self._rowSelection = None
+        self._colSelection = None
+        self._structure = None
+        opts = {k: v for k, v in options.items()
+                if k not in ('optimize', 'maxStage', 'rows', 'cols')}
+        self._init_properties(c.size, c.size, np.complex128, **opts)
+
+    @property
+    def tenC(self):
+        return self._tenC
+
+    @property
+    def vecC(self):
+        return self._tenC
+
+    @property
+    def content(self):
+        if self._structure is None:
+            n = self._tenC.size
+            L = fftsize.circulant_length(n, self._optimize, self._maxStage)
+            c = self._tenC
+            if L != n:
+                c = np.concatenate([c, np.zeros(L - 2 * n + 1, c.dtype),
+                                    c[1:]])
+            F = Fourier(L, optimize=self._optimize, maxStage=self._maxStage)
+            spec = F.forward(c) / L
+            self._structure = (Product(Hermitian(F), Diag(spec), F),)
+        return self._structure
+
+    @property
+    def rowSelection(self):
+        return np.arange(self.numRows)
+
+    @property
+    def colSelection(self):
+        return np.arange(self.numCols)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_CIRCULANT, self, vec0=self._tenC)
+
+    def _reference(self):
+        n = self._tenC.size
+        i = np.arange(n)
+        return self._tenC[(i[:, None] - i[None, :]) % n].astype(self.dtype)
+
+
+class Toeplitz(Partial):
+    """Toeplitz matrix (fastmat/Toeplitz.pyx:31-734), 1-level.
+
+    ``Toeplitz(vecC, vecR)``: first column vecC and first row
+    [vecC[0], vecR[-1], vecR[-2], ...] (T[0, j] = vecR[-j]);
+    ``Toeplitz(tenT, split=n_rows)`` with tenT = [vecC, vecR]."""
+
+    def __init__(self, *args, **options):
+        split = options.pop('split', None)
+        if len(args) == 2:
+            if not all(isinstance(a, np.ndarray) for a in args):
+                raise ValueError(
+                    "You must specify two 1D-ndarrays containing the " +
+                    "column- and row-definition vectors or one ndarray tensor")
+            if split is not None:
+                raise ValueError(
+                    "You must not define split points when supplying " +
+                    "column- and row-definition vectors.")
+            dt = np.promote_types(args[0].dtype, args[1].dtype)
+            vc = np.atleast_1d(np.squeeze(args[0].astype(dt)))
+            vr = np.atleast_1d(np.squeeze(args[1].astype(dt)))
+            if vc.ndim != 1 or vr.ndim > 1:
+                raise ValueError(
+                    "Column- and row-definition vectors must be 1D.")
+            vr = vr.reshape(-1)
+            tenT = np.hstack((vc, vr))
+            split = vc.size
+        elif len(args) == 1:
+            tenT = np.asarray(args[0])
+            if tenT.ndim != 1:
+                raise NotImplementedError(
+                    "multi-level Toeplitz is not supported by fastmat_gb300")
+            if split is None:
+                if (tenT.size + 1) % 2 != 0:
+                    raise ValueError(
+                        "Defining a tensor with non-square levels requires " +
+                        "explicit split points.")
+                split = (tenT.size + 1) // 2
+            split = int(np.atleast_1d(split)[0])
+            if split < 1 or split > tenT.size:
+                raise ValueError(
+                    "Entry in split vector outside of defining tensor bounds")
+        else:
+            raise ValueError(
+                "Invalid number of arguments to Toeplitz: Expecting exactly " +
+                "one or two fixed arguments")
+        self._tenT = tenT.astype(np.complex128)
+        self._split = split
+        nr = split
+        nc = tenT.size - nr + 1
+        self._optimize = options.get('optimize', True)
+        self._maxStage = options.get('maxStage', 4)
+        self._rowSelection = None
+        self._colSelection = None
+        opts = {k: v for k, v in options.items()
+                if k not in ('optimize', 'maxStage', 'rows', 'cols')}
+        self._init_properties(nr, nc, np.complex128, **opts)
+
+    @property
+    def tenT(self):
+        return self._tenT
+
+    @property
+    def vecC(self):
+        return self._tenT[:self._split]
+
+    @property
+    def vecR(self):
+        return self._tenT[self._split:]
+
+    @property
+    def content(self):
+        raise NotImplementedError(
+            "Toeplitz content structure is not materialised by "
+            "fastmat_gb300")
+
+    @property
+    def rowSelection(self):
+        return np.arange(self.numRows)
+
+    @property
+    def colSelection(self):
+        return np.arange(self.numCols)
+
+    def _emit(self, b):
+        return b.add(_native.NODE_TOEPLITZ, self, vec0=self.vecC,
+                     vec1=self.vecR)
+
+    def _reference(self):
+        nr, nc = self.shape
+        d = np.arange(nr)[:, None] - np.arange(nc)[None, :]
+        full = np.concatenate([self.vecR, self.vecC])
+        return full[d + nc - 1].astype(self.dtype)

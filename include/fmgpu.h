@@ -1,0 +1,178 @@
+/*
+ * fmgpu.h -- C ABI of the GB300 (sm_103a) structured-operator matvec engine.
+ *
+ * The engine replaces the compute behind fastmat's Matrix.forward /
+ * Matrix.backward for Circulant, Toeplitz, Fourier, Hadamard, Kron and the
+ * Diag / Partial / Permutation / Product / Sum / Hermitian / Conjugate
+ * compositions that chain them.  An operator tree is described to the library
+ * as a flat array of fm_node records; the library compiles it into a plan
+ * (a short list of fused CUDA launches plus the device constants they read)
+ * that is executed on column-major (Fortran-order) data, one column per
+ * right-hand side, exactly as fastmat lays out its 2-D arrays.
+ *
+ * Every entry point returns an int status (FM_OK == 0).  On failure
+ * fm_last_error() returns a message for the calling thread.  Nothing in this
+ * interface uses C++ or torch types.
+ *
+ * Reference interfaces replaced (paths relative to the fastmat project root):
+ *   fm_plan_create   <- the operator constructors that precompute transform
+ *                       state: Fourier.__init__ (fastmat/Fourier.pyx:63-161),
+ *                       Circulant.__init__ (fastmat/Circulant.pyx:63-227),
+ *                       Toeplitz.__init__ (fastmat/Toeplitz.pyx:79-322),
+ *                       Hadamard.__init__ (fastmat/Hadamard.pyx:113-133),
+ *                       Kron.__init__ (fastmat/Kron.pyx:79-129)
+ *   fm_execute       <- Matrix.forward / Matrix.backward and the _forwardC /
+ *                       _backwardC hooks they dispatch to
+ *                       (fastmat/Matrix.pyx:1819-1829, 1844-1910,
+ *                        1912-1922, 1937-2007)
+ *   fm_execute_host  <- the same, called with host (numpy) buffers as
+ *                       fastmat's _forwardC(arrX, arrRes, ...) receives them
+ *                       (fastmat/Matrix.pyx:1892-1901)
+ *   fm_plan_destroy  <- instance deallocation (operators are immutable,
+ *                       fastmat/Matrix.pyx:341-358)
+ */
+#ifndef FMGPU_H
+#define FMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FM_OK 0
+#define FM_ERR_VALUE 1        /* bad shape / argument   -> ValueError        */
+#define FM_ERR_TYPE 2         /* unsupported dtype      -> TypeError         */
+#define FM_ERR_UNSUPPORTED 3  /* not implemented case   -> NotImplementedError*/
+#define FM_ERR_CUDA 4         /* CUDA runtime failure   -> RuntimeError      */
+#define FM_ERR_NOMEM 5        /* device allocation fail -> MemoryError       */
+#define FM_ERR_TIMEOUT 6      /* a bounded device wait gave up               */
+
+/* ---- element types: same numbering as fastmat's ftype
+ *      (fastmat/core/types.pxd:45-55) ------------------------------------- */
+#define FM_I8 0
+#define FM_I16 1
+#define FM_I32 2
+#define FM_I64 3
+#define FM_F32 4
+#define FM_F64 5
+#define FM_C64 6
+#define FM_C128 7
+
+/* ---- operator node kinds ------------------------------------------------ */
+#define FM_NODE_FOURIER 1      /* n = order                                   */
+#define FM_NODE_CIRCULANT 2    /* vec0 = defining column c (len0 = n)         */
+#define FM_NODE_TOEPLITZ 3     /* vec0 = column (len0 = rows), vec1 = row
+                                  vector (len1 = cols - 1), fastmat order
+                                  T[0, j] = vecR[-j]                          */
+#define FM_NODE_HADAMARD 4     /* n = order (size 2^n)                        */
+#define FM_NODE_DIAG 5         /* vec0 = diagonal                             */
+#define FM_NODE_PARTIAL 6      /* one child; vec0 = row indices (int64) or
+                                  NULL, vec1 = column indices (int64) or NULL */
+#define FM_NODE_PERMUTATION 7  /* vec0 = sigma (int64)                        */
+#define FM_NODE_PRODUCT 8      /* children applied right to left, times
+                                  (scalar_re + i scalar_im)                   */
+#define FM_NODE_SUM 9          /* children summed                             */
+#define FM_NODE_KRON 10        /* children = square factors, factor 0 is the
+                                  most significant index (np.kron order)      */
+#define FM_NODE_HERMITIAN 11   /* one child; forward <-> backward             */
+#define FM_NODE_CONJUGATE 12   /* one child; conj o child o conj              */
+#define FM_NODE_EYE 13         /* identity of size rows                       */
+#define FM_NODE_DENSE 14       /* vec0 = rows x cols matrix, column-major     */
+
+typedef struct fm_node {
+    int32_t kind;
+    int32_t dtype;          /* the operator's fastmat dtype (FM_*)            */
+    int64_t rows, cols;     /* operator shape                                 */
+    int32_t first_child;    /* index into the children array                  */
+    int32_t num_children;
+    int64_t n;              /* kind-specific size (order, ...)                */
+    const void *vec0;       /* host pointer, kind-specific, copied at create  */
+    int64_t len0;
+    int32_t type0;          /* FM_* element type of vec0                      */
+    int32_t pad0;
+    const void *vec1;
+    int64_t len1;
+    int32_t type1;
+    int32_t pad1;
+    double scalar_re, scalar_im;
+} fm_node;
+
+/* plan precisions */
+#define FM_PREC_NATIVE 0  /* compute in the operator/input promoted type     */
+#define FM_PREC_FP32 1    /* opt-in: float32 / complex64 arithmetic          */
+
+/* directions */
+#define FM_FORWARD 0
+#define FM_BACKWARD 1
+
+typedef struct fm_plan fm_plan;
+
+/* Compile an operator tree.  `compute_type` is the element type the plan
+ * computes and stores intermediates in (FM_F32, FM_F64, FM_C64, FM_C128 or
+ * FM_I64 for integer-only trees).  Node vectors are host pointers, copied
+ * during the call; the caller may free them afterwards.  Device constants
+ * (spectra, chirps, twiddles, index maps) are built on the current device. */
+int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
+                   const int32_t *children, int32_t num_children,
+                   int32_t root, int32_t compute_type, fm_plan **out_plan);
+
+/* y = A x (FM_FORWARD) or y = A^H x (FM_BACKWARD) on `num_cols` columns.
+ * x and y are DEVICE pointers, column-major with leading dimensions ld_x /
+ * ld_y (in elements).  x may have any FM_* element type (it is converted in
+ * the first launch); y has element type y_type.  x is never written.  x and y
+ * must not overlap.  Runs asynchronously on `stream` (a cudaStream_t, NULL =
+ * default stream); a plan must not run on two streams at once. */
+int fm_execute(fm_plan *plan, int32_t direction,
+               const void *x, int32_t x_type, int64_t ld_x,
+               void *y, int32_t y_type, int64_t ld_y,
+               int64_t num_cols, void *stream);
+
+/* Same as fm_execute, but records a CUDA event around every launch and
+ * writes each launch's elapsed milliseconds into ms[0 .. *num_launches-1]
+ * (capacity given in *num_launches on entry).  Synchronises the stream.
+ * Instrumentation for benchmarks; it has no counterpart in the reference. */
+int fm_execute_profiled(fm_plan *plan, int32_t direction,
+                        const void *x, int32_t x_type, int64_t ld_x,
+                        void *y, int32_t y_type, int64_t ld_y,
+                        int64_t num_cols, void *stream, float *ms,
+                        int32_t *num_launches);
+
+/* Same as fm_execute with HOST buffers: copies x to the device, runs the
+ * plan and copies the result back into y before returning (synchronous). */
+int fm_execute_host(fm_plan *plan, int32_t direction,
+                    const void *x, int32_t x_type, int64_t ld_x,
+                    void *y, int32_t y_type, int64_t ld_y,
+                    int64_t num_cols);
+
+int fm_plan_destroy(fm_plan *plan);
+
+/* Plan introspection for tests and benchmarks. */
+typedef struct fm_plan_info {
+    int64_t rows, cols;          /* operator shape                           */
+    int32_t num_launches_fwd;    /* kernel launches per forward call         */
+    int32_t num_launches_bwd;
+    int64_t scratch_bytes_per_col; /* device scratch a column needs          */
+    int64_t const_bytes;         /* device constants owned by the plan       */
+    int32_t compute_type;
+    int32_t pad;
+} fm_plan_info;
+int fm_plan_get_info(const fm_plan *plan, fm_plan_info *info);
+
+/* Human-readable dump of the lowered launches (stage list) into buf. */
+int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
+                     int64_t buf_len);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *fm_last_error(void);
+
+/* ABI version (major * 100 + minor). */
+int32_t fm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FMGPU_H */

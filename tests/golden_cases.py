@@ -48,7 +48,14 @@ def load_circulant1024():
     return np.load(os.path.join(HERE, 'circulant1024.npz'))
 
 
-def tolerance(ref, x, case_dtype=None):
+#: cases where the reference itself is less accurate than 1e-12: fastmat's
+#: Bluestein chirp forms the phase n^2 pi / N in float64
+#: (fastmat/Fourier.pyx:130-146), which costs ~1e-12 at N = 4099; these are
+#: held to the exact DFT separately.
+REFERENCE_ERROR = {'fourier_4099': 5e-12}
+
+
+def tolerance(ref, x, case_dtype=None, name=None):
     """Accuracy bound for a result against a reference output.
 
     Double-precision results are held to 1e-12 relative error (fastmat's
@@ -62,4 +69,4 @@ def tolerance(ref, x, case_dtype=None):
     if single:
         n = max(ref.shape[0], x.shape[0])
         return 5 * 2.0 * np.finfo(np.float32).eps * 2.0 * np.sqrt(n)
-    return 1e-12
+    return REFERENCE_ERROR.get(name, 1e-12)

@@ -1,0 +1,113 @@
+"""GPU parity against the reference's own outputs (golden fixtures) and the
+CPU oracle, for every operator case in tests/golden/operators.npz."""
+
+import numpy as np
+import pytest
+
+from oracle import fm_oracle as fo
+from tests.golden_cases import (REFERENCE_ERROR, load_cases,
+                                load_circulant1024, tolerance)
+
+pytestmark = pytest.mark.gpu
+
+CASES = load_cases()
+
+
+def _ns():
+    import fastmat_gb300 as fg
+    return dict(Fourier=fg.Fourier, Circulant=fg.Circulant,
+                Toeplitz=fg.Toeplitz, Hadamard=fg.Hadamard, Kron=fg.Kron,
+                Diag=fg.Diag, Partial=fg.Partial,
+                Permutation=fg.Permutation, Product=fg.Product, Sum=fg.Sum,
+                Hermitian=fg.Hermitian, Conjugate=fg.Conjugate,
+                Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix, np=np)
+
+
+ONS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
+           Hadamard=fo.Hadamard, Kron=fo.Kron, Diag=fo.Diag,
+           Partial=fo.Partial, Permutation=fo.Permutation,
+           Product=fo.Product, Sum=fo.Sum, Hermitian=fo.Hermitian,
+           Conjugate=fo.Conjugate, Transpose=fo.Transpose, Eye=fo.Eye,
+           Matrix=fo.Dense, np=np)
+
+
+def _close(out, ref, x, name=None):
+    if np.issubdtype(ref.dtype, np.integer):
+        return np.array_equal(out, ref)
+    return fo.rel_err(out, ref) <= tolerance(ref, x, name=name)
+
+
+@pytest.mark.parametrize('case', CASES, ids=lambda c: c.name)
+def test_gpu_matches_reference_and_oracle(case):
+    op = case.build(_ns())
+    oop = case.build(ONS)
+    x_before = case.x.copy()
+    y = op.forward(case.x)
+    z = op.backward(case.g)
+    # inputs are never modified (fastmat/inspect/test.py:336-338)
+    assert np.array_equal(case.x, x_before)
+    # fastmat's output type contract
+    want = np.dtype(fo.promote(case.dtype, case.x.dtype))
+    assert y.dtype == want and z.dtype == np.dtype(
+        fo.promote(case.dtype, case.g.dtype))
+    assert y.shape == case.fwd.shape and z.shape == case.bwd.shape
+    assert y.flags.f_contiguous
+    # against the reference's outputs
+    assert _close(y, case.fwd, case.x, case.name), fo.rel_err(y, case.fwd)
+    assert _close(z, case.bwd, case.g, case.name), fo.rel_err(z, case.bwd)
+    if case.name in REFERENCE_ERROR:
+        # the GPU result is held to the exact DFT instead
+        assert fo.rel_err(y, np.fft.fft(case.x, axis=0)) <= 1e-12
+    # against the oracle (double precision wherever the output is double)
+    yo, zo = oop.forward(case.x), oop.backward(case.g)
+    if np.issubdtype(yo.dtype, np.integer):
+        assert np.array_equal(y, yo) and np.array_equal(z, zo)
+    else:
+        single = y.dtype in (np.complex64, np.float32)
+        tol = (tolerance(yo.astype(y.dtype), case.x) if single
+               else REFERENCE_ERROR.get(case.name, 1e-12))
+        assert fo.rel_err(y, yo) <= tol, fo.rel_err(y, yo)
+        assert fo.rel_err(z, zo) <= tol, fo.rel_err(z, zo)
+
+
+@pytest.mark.parametrize('case', [c for c in CASES if c.x.shape[1] > 1][:12],
+                         ids=lambda c: c.name)
+def test_gpu_one_dimensional_input(case):
+    op = case.build(_ns())
+    y = op.forward(case.x[:, 0])
+    assert y.ndim == 1
+    assert _close(y, case.fwd[:, 0], case.x)
+
+
+def test_circulant1024_workload():
+    import fastmat_gb300 as fg
+    g = load_circulant1024()
+    C = fg.Circulant(g['c'])
+    y = C.forward(g['x'])
+    z = C.backward(g['x'])
+    assert fo.rel_err(y, g['fwd']) <= 1e-12
+    assert fo.rel_err(z, g['bwd']) <= 1e-12
+    assert fo.rel_err(y, C.reference() @ g['x']) <= 1e-12
+
+
+def test_device_tensor_path():
+    import torch
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(3)
+    c = rng.standard_normal(300) + 1j * rng.standard_normal(300)
+    x = rng.standard_normal((300, 5)) + 1j * rng.standard_normal((300, 5))
+    C = fg.Circulant(c)
+    xt = torch.from_numpy(x).cuda()
+    yt = C.forward(xt)
+    assert yt.is_cuda and tuple(yt.shape) == (300, 5)
+    assert fo.rel_err(yt.cpu().numpy(), fo.Circulant(c).forward(x)) <= 1e-12
+    y1 = C.backward(xt[:, 2])
+    assert tuple(y1.shape) == (300,)
+    assert fo.rel_err(y1.cpu().numpy(),
+                      fo.Circulant(c).backward(x[:, 2])) <= 1e-12
+
+
+def test_empty_columns():
+    import fastmat_gb300 as fg
+    y = fg.Fourier(16).forward(np.zeros((16, 0)))
+    assert y.shape == (16, 0) and y.dtype == np.complex128
