@@ -66,7 +66,7 @@ class FmPlanInfo(ctypes.Structure):
 
 #: every entry point include/fmgpu.h declares
 EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
-           'fm_execute_host',
+           'fm_execute_static', 'fm_execute_host',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
            'fm_last_error', 'fm_version')
 
@@ -103,6 +103,9 @@ def load(build_if_missing=True):
             P, I32, P, I32, I64, P, I32, I64, I64, P,
             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I32)]
         lib.fm_execute_profiled.restype = ctypes.c_int
+        lib.fm_execute_static.argtypes = [P, I32, P, I32, I64, P, I32, I64,
+                                          I64, P]
+        lib.fm_execute_static.restype = ctypes.c_int
         lib.fm_execute_host.argtypes = [P, I32, P, I32, I64, P, I32, I64, I64]
         lib.fm_execute_host.restype = ctypes.c_int
         lib.fm_plan_destroy.argtypes = [P]

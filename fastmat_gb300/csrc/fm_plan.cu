@@ -21,6 +21,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1229,6 +1230,91 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
   return FM_OK;
 }
 
+// ------------------------------------------------------------ static scratch
+// Scratch for fm_execute_static: a fixed array in device memory, reserved by
+// every GPU that loads this library for as long as the process lives, so that
+// callers which must not allocate device memory during a call can still run
+// the multi-launch plans (long four-step transforms, Sum) that keep
+// intermediates between launches.
+static __device__ __align__(256) unsigned char
+    g_static_scratch[FM_STATIC_SCRATCH_BYTES];
+
+// Device address of g_static_scratch, looked up once per device (host code
+// cannot use the symbol's name as an address).
+void *static_scratch_address() {
+  static std::mutex mu;
+  static std::map<int, void *> addr;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = addr.find(dev);
+  if (it != addr.end()) return it->second;
+  void *p = nullptr;
+  CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+  addr[dev] = p;
+  return p;
+}
+
+// The launch loop of run_plan with every scratch buffer placed in the static
+// array; returns FM_ERR_VALUE before launching anything if the plan needs
+// more scratch than the array holds.
+int run_plan_static(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
+                    void *y, int y_type, i64 ld_y, i64 M, cudaStream_t s) {
+  if (M <= 0) return FM_OK;
+  const size_t align = 256;
+  std::vector<size_t> offs(P->scratch_rows.size());
+  size_t total = 0;
+  for (size_t k = 0; k < P->scratch_rows.size(); ++k) {
+    offs[k] = total;
+    total += ((size_t)P->scratch_rows[k] * M * P->esz + align - 1) / align *
+             align;
+  }
+  if (total > (size_t)FM_STATIC_SCRATCH_BYTES)
+    fail(FM_ERR_VALUE,
+         "fm_execute_static: this call needs " + std::to_string(total) +
+             " bytes of scratch, more than the " +
+             std::to_string((size_t)FM_STATIC_SCRATCH_BYTES) +
+             "-byte static array; use fewer columns or fm_execute");
+  char *base = total ? (char *)static_scratch_address() : nullptr;
+  for (const LStep &ls : P->steps[dir]) {
+    fmk::Step st = ls.st;
+    auto bind = [&](int id, const void *&ptr, int &type, i64 &ld) {
+      if (id == 0) {
+        ptr = x;
+        type = x_type;
+        ld = ld_x;
+      } else if (id == 1) {
+        ptr = y;
+        type = y_type;
+        ld = ld_y;
+      } else {
+        ptr = base + offs[id - 2];
+        type = P->ctype;
+        ld = P->scratch_rows[id - 2];
+      }
+    };
+    const void *sp;
+    const void *dp;
+    bind(ls.src, sp, st.src_type, st.ld_src);
+    bind(ls.dst, dp, st.dst_type, st.ld_dst);
+    st.src = sp;
+    st.dst = const_cast<void *>(dp);
+    st.num_cols = M;
+    const i64 grid = (st.V * M + st.B - 1) / st.B;
+    if (grid > 0x7fffffffLL) fail(FM_ERR_VALUE, "too many columns");
+    cudaError_t e;
+    switch (P->ctype) {
+      case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+      default: e = fmk::launch_c128(st, ls.cls, ls.threads, ls.smem, grid, s); break;
+    }
+    CUDA_TRY(e);
+  }
+  return FM_OK;
+}
+
 const char *kind_name(int k) {
   switch (k) {
     case fmk::OP_FFT: return "fft";
@@ -1357,6 +1443,26 @@ int fm_execute_profiled(fm_plan *plan, int32_t direction, const void *x,
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return st;
+  });
+}
+
+int fm_execute_static(fm_plan *plan, int32_t direction, const void *x,
+                      int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
+                      int64_t ld_y, int64_t num_cols, void *stream) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    if (!valid_type(x_type) || !valid_type(y_type))
+      fail(FM_ERR_TYPE, "unsupported element type");
+    const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
+    const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
+    if (num_cols < 0) fail(FM_ERR_VALUE, "negative column count");
+    if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "NULL data pointer");
+    if (ld_x < n_in || ld_y < n_out)
+      fail(FM_ERR_VALUE, "leading dimension smaller than the vector size");
+    return run_plan_static(plan, direction, x, x_type, ld_x, y, y_type, ld_y,
+                           num_cols, (cudaStream_t)stream);
   });
 }
 

@@ -140,6 +140,38 @@ int fm_execute_profiled(fm_plan *plan, int32_t direction,
                         int64_t num_cols, void *stream, float *ms,
                         int32_t *num_launches);
 
+/* ---- execution without device allocation ------------------------------
+ * fm_execute_static runs a plan exactly like fm_execute, but never allocates
+ * device memory during the call.  It exists for callers that must not call
+ * cudaMalloc/cudaFree while they run: code that works inside a fixed memory
+ * budget because another allocator (for example a framework's caching
+ * allocator) has already reserved the device memory, and latency-critical
+ * loops that cannot afford the device-wide synchronisation those calls
+ * imply.  fm_execute instead grows a per-plan scratch buffer with cudaMalloc
+ * the first time a plan runs on more columns than before.
+ *
+ * The scratch that multi-launch plans keep between launches (long
+ * four-step transforms, Sum) is taken from one fixed array of
+ * FM_STATIC_SCRATCH_BYTES (16 MiB) compiled into the library; every GPU that
+ * loads the library reserves it until the process exits.  A call whose plan
+ * needs more scratch for `num_cols` columns than the array holds returns
+ * FM_ERR_VALUE without launching anything.  Plans that need no scratch use
+ * none of it.
+ *
+ * All calls share the one array per device and it keeps whatever the last
+ * call left in it; every launch writes the scratch it reads first, so
+ * nothing has to be cleared between calls.  Calls whose work overlaps on the
+ * GPU (for example on two streams) race on the array: order them.  The first
+ * call on each device looks up the array's device address (host code cannot
+ * use the symbol directly); make that first call before any stream capture.
+ * The plan itself is built beforehand by fm_plan_create, which does
+ * allocate.  This entry point has no counterpart in the reference. */
+#define FM_STATIC_SCRATCH_BYTES (16u << 20)
+int fm_execute_static(fm_plan *plan, int32_t direction,
+                      const void *x, int32_t x_type, int64_t ld_x,
+                      void *y, int32_t y_type, int64_t ld_y,
+                      int64_t num_cols, void *stream);
+
 /* Same as fm_execute with HOST buffers: copies x to the device, runs the
  * plan and copies the result back into y before returning (synchronous). */
 int fm_execute_host(fm_plan *plan, int32_t direction,
