@@ -66,7 +66,7 @@ class FmPlanInfo(ctypes.Structure):
 
 #: every entry point include/fmgpu.h declares
 EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
-           'fm_execute_static', 'fm_execute_host',
+           'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
            'fm_last_error', 'fm_version')
 
@@ -108,6 +108,8 @@ def load(build_if_missing=True):
         lib.fm_execute_static.restype = ctypes.c_int
         lib.fm_execute_host.argtypes = [P, I32, P, I32, I64, P, I32, I64, I64]
         lib.fm_execute_host.restype = ctypes.c_int
+        lib.fm_plan_check.argtypes = [P]
+        lib.fm_plan_check.restype = ctypes.c_int
         lib.fm_plan_destroy.argtypes = [P]
         lib.fm_plan_destroy.restype = ctypes.c_int
         lib.fm_plan_get_info.argtypes = [P, ctypes.POINTER(FmPlanInfo)]
@@ -178,6 +180,10 @@ class Plan:
             self.handle, direction, x.ctypes.data, DTYPE_CODE[x.dtype],
             x.shape[0], y.ctypes.data, DTYPE_CODE[y.dtype], y.shape[0],
             x.shape[1]))
+
+    def check(self):
+        """Raise if a kernel of this plan reported a failure (syncs)."""
+        check(self._lib.fm_plan_check(self.handle))
 
     def info(self):
         inf = FmPlanInfo()

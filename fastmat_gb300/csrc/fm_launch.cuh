@@ -9,16 +9,16 @@
 
 namespace fmk {
 
-cudaError_t launch_f32(const Step &st, int cls, int threads, size_t smem,
-                       i64 grid, cudaStream_t s);
-cudaError_t launch_f64(const Step &st, int cls, int threads, size_t smem,
-                       i64 grid, cudaStream_t s);
-cudaError_t launch_c64(const Step &st, int cls, int threads, size_t smem,
-                       i64 grid, cudaStream_t s);
-cudaError_t launch_c128(const Step &st, int cls, int threads, size_t smem,
-                       i64 grid, cudaStream_t s);
-cudaError_t launch_i64(const Step &st, int cls, int threads, size_t smem,
-                       i64 grid, cudaStream_t s);
+cudaError_t launch_f32(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_f64(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_c64(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_c128(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_i64(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
 
 // maximum dynamic shared memory a launch may request (GB300: 227 KB / CTA)
 constexpr int kMaxSmem = 227 * 1024;

@@ -28,6 +28,8 @@
 #include "../../include/fmgpu.h"
 #include "fm_launch.cuh"
 
+#include <cuda.h>
+
 using fmk::i64;
 typedef std::complex<double> cd;
 
@@ -181,6 +183,12 @@ struct LStep {
   int src, dst;  // 0 = x, 1 = y, >= 2 scratch
   int cls, threads;
   size_t smem;
+  int lay = 0;                     // tile layout (1: element-major)
+  int tma_in_ok = 0, tma_out_ok = 0;  // views allow TMA boxes
+  // last encoded tensor maps and the (address, ld, columns) they describe
+  const void *tm_in_key = nullptr, *tm_out_key = nullptr;
+  i64 tm_in_ld = -1, tm_out_ld = -1, tm_in_m = -1, tm_out_m = -1;
+  CUtensorMap tm_in, tm_out;
 };
 
 }  // namespace
@@ -202,6 +210,7 @@ struct fm_plan {
   void *dx = nullptr, *dy = nullptr;
   size_t dx_cap = 0, dy_cap = 0;
   cudaStream_t hstream = nullptr;
+  int *err = nullptr;  // device status word written by bounded waits
   ~fm_plan();
 };
 
@@ -269,7 +278,7 @@ class Planner {
   Planner(fm_plan *P, const std::vector<NodeRec> &nodes)
       : P_(P), nodes_(nodes) {
     cplx_ = is_cplx(P->ctype);
-    ept_ = P->esz >= 16 ? 8 : 16;
+    ept_ = P->esz == 4 ? 16 : 8;
     lmax_ = (i64)ept_ * FM_MAX_THREADS;
   }
 
@@ -435,6 +444,129 @@ class Planner {
     return p;
   }
 
+  // ---------------------------------------------------------- FFT order
+  // The device FFT runs in place: DIF leaves the spectrum in digit-reversed
+  // order for its radix sequence, DIT takes that order back to natural.
+  // nat[P] is the natural index stored at position P, pos its inverse.
+  struct Perm {
+    std::vector<int> nat, pos;
+    const int *nat_dev = nullptr, *pos_dev = nullptr;
+  };
+  std::map<std::vector<int>, Perm> perms_;
+
+  const Perm &perm_for(const std::vector<int> &rad) {
+    auto it = perms_.find(rad);
+    if (it != perms_.end()) return it->second;
+    int L = 1;
+    for (int r : rad) L *= r;
+    Perm pm;
+    pm.nat.assign(L, 0);
+    pm.pos.assign(L, 0);
+    std::vector<int> k(rad.size(), 0);
+    for (int c = 0; c < L; ++c) {
+      // digits k (k[0] most significant in the position)
+      int posv = 0, natv = 0, mul = 1;
+      for (size_t i = 0; i < rad.size(); ++i) posv = posv * rad[i] + k[i];
+      for (size_t i = 0; i < rad.size(); ++i) {
+        natv += k[i] * mul;
+        mul *= rad[i];
+      }
+      pm.nat[posv] = natv;
+      pm.pos[natv] = posv;
+      for (int i = (int)rad.size() - 1; i >= 0; --i) {
+        if (++k[i] < rad[i]) break;
+        k[i] = 0;
+      }
+    }
+    void *a = dalloc(L * sizeof(int));
+    void *b = dalloc(L * sizeof(int));
+    CUDA_TRY(cudaMemcpy(a, pm.nat.data(), L * sizeof(int),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b, pm.pos.data(), L * sizeof(int),
+                        cudaMemcpyHostToDevice));
+    pm.nat_dev = (const int *)a;
+    pm.pos_dev = (const int *)b;
+    return perms_.emplace(rad, pm).first->second;
+  }
+
+  std::vector<int> op_radices(const fmk::Op &o) {
+    return std::vector<int>(o.rad, o.rad + o.nrad);
+  }
+
+  // Lower abstract FFT ops of a program to DIF/DIT, keeping track of the
+  // element order; returns the storer's position table if the program ends
+  // in digit-reversed order (nullptr otherwise).
+  const int *finalize(std::vector<fmk::Op> &ops) {
+    std::vector<fmk::Op> out;
+    bool permuted = false;
+    std::vector<int> cur;
+    auto to_natural = [&]() {
+      const Perm &pm = perm_for(cur);
+      std::vector<i64> m(pm.pos.begin(), pm.pos.end());
+      out.push_back(gather_op(m));
+      permuted = false;
+    };
+    for (fmk::Op o : ops) {
+      switch (o.kind) {
+        case fmk::OP_FFT: {
+          std::vector<int> rad = op_radices(o);
+          if (permuted && rad != cur) to_natural();
+          if (!permuted) {
+            o.kind = fmk::OP_DIF;
+            permuted = true;
+            cur = rad;
+          } else {
+            o.kind = fmk::OP_DIT;
+            permuted = false;
+          }
+          out.push_back(o);
+          break;
+        }
+        case fmk::OP_MUL: {
+          if (permuted) {
+            const Perm &pm = perm_for(cur);
+            const std::vector<cd> &v = host_vec_.at(o.ptr);
+            std::vector<cd> w(v);
+            const i64 len = o.len;
+            const i64 rows = o.stride > 0 ? (i64)v.size() / o.stride : 1;
+            const i64 rs = o.stride > 0 ? o.stride : 0;
+            for (i64 r = 0; r < rows; ++r)
+              for (i64 P = 0; P < len; ++P)
+                w[r * rs + P] = v[r * rs + pm.nat[P]];
+            o.ptr = upload(w);
+          }
+          out.push_back(o);
+          break;
+        }
+        case fmk::OP_GATHER: {
+          if (permuted) {
+            const Perm &pm = perm_for(cur);
+            const std::vector<i64> &m = host_map_.at(o.ptr);
+            std::vector<i64> c(m.size());
+            for (size_t i = 0; i < m.size(); ++i)
+              c[i] = m[i] < 0 ? -1 : pm.pos[m[i]];
+            o.ptr = upload_map(c);
+            permuted = false;
+          }
+          out.push_back(o);
+          break;
+        }
+        case fmk::OP_TW:
+          if (permuted) o.ptr2 = perm_for(cur).nat_dev;
+          out.push_back(o);
+          break;
+        case fmk::OP_CONJ:
+        case fmk::OP_SCALE: out.push_back(o); break;
+        default:
+          if (permuted) to_natural();
+          out.push_back(o);
+          break;
+      }
+    }
+    ops.swap(out);
+    return permuted ? perm_for(cur).pos_dev : nullptr;
+  }
+
   // ---------------------------------------------------------- FFT helpers
   std::vector<int> radices(i64 n) {
     std::vector<int> r;
@@ -443,7 +575,7 @@ class Planner {
         r.push_back(p);
         n /= p;
       }
-    const int big = ept_ >= 16 ? 16 : 8;
+    const int big = 16;
     while (n % big == 0) {
       r.push_back(big);
       n /= big;
@@ -473,7 +605,7 @@ class Planner {
     fmk::Op o = mkop(fmk::OP_FWHT, (int)n);
     int bits = 0;
     while ((1LL << bits) < n) ++bits;
-    const int g = ept_ >= 16 ? 4 : 3;
+    const int g = 4;
     while (bits > 0) {
       const int k = std::min(g, bits);
       o.rad[o.nrad++] = (unsigned char)k;
@@ -919,7 +1051,8 @@ class Planner {
   int kernel_class(const std::vector<fmk::Op> &ops) {
     bool fft = false, odd = false, fwht = false, gen = false;
     for (const fmk::Op &o : ops) {
-      if (o.kind == fmk::OP_FFT) {
+      if (o.kind == fmk::OP_FFT || o.kind == fmk::OP_DIF ||
+          o.kind == fmk::OP_DIT) {
         fft = true;
         for (int i = 0; i < o.nrad; ++i)
           if (o.rad[i] & 1) odd = true;
@@ -933,14 +1066,43 @@ class Planner {
     return 3;
   }
 
+  // whether lowering the FFTs of a program to DIF/DIT needs an explicit
+  // reordering gather (an order-sensitive op follows a digit-reversed FFT)
+  static bool needs_gather(const std::vector<fmk::Op> &ops) {
+    bool permuted = false;
+    std::vector<int> cur;
+    for (const fmk::Op &o : ops) {
+      switch (o.kind) {
+        case fmk::OP_FFT: {
+          std::vector<int> rad(o.rad, o.rad + o.nrad);
+          if (permuted && rad != cur) return true;
+          permuted = !permuted;
+          cur = rad;
+          break;
+        }
+        case fmk::OP_GATHER: permuted = false; break;
+        case fmk::OP_MUL:
+        case fmk::OP_TW:
+        case fmk::OP_CONJ:
+        case fmk::OP_SCALE: break;
+        default:
+          if (permuted) return true;
+          break;
+      }
+    }
+    return false;
+  }
+
   // longest working length a program of this op mix may use in one tile
   i64 limit_for(const std::vector<fmk::Op> &ops) {
-    const int cls = kernel_class(ops);
+    const int cls = needs_gather(ops) ? 0 : kernel_class(ops);
     return (cls == 0 || cls == 2) ? lmax_ / 2 : lmax_;
   }
 
-  void finish(LStep &ls, const std::vector<fmk::Op> &ops) {
+  void finish(LStep &ls, const std::vector<fmk::Op> &ops_in) {
     fmk::Step &st = ls.st;
+    std::vector<fmk::Op> ops = ops_in;
+    st.out_pos = finalize(ops);
     if ((int)ops.size() > FM_MAX_OPS)
       fail(FM_ERR_UNSUPPORTED, "operator chain too long for one launch");
     st.nops = (int)ops.size();
@@ -949,36 +1111,77 @@ class Planner {
     bool odd = ls.cls == 2 || ls.cls == 0;
     const int ept = odd ? ept_ / 2 : ept_;
     const int L = std::max(st.L, 1);
-    int Lp = fmk::pidx<float2>(0);  // placeholder, recomputed below
-    const int shift = P_->esz >= 16 ? 3 : (P_->esz == 8 ? 4 : 5);
-    Lp = (L - 1) + ((L - 1) >> shift) + 1;
-    if ((Lp & 1) == 0) ++Lp;
-    st.Lp = Lp;
-    const i64 nvec = st.V;  // per column; tiles may span columns
-    const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
-    int B = 1;
-    if (strided) {
-      const int coal = std::max(1, 128 / P_->esz);
-      B = coal;
-    }
+    const int esz = P_->esz;
     auto threads_for = [&](int b) {
       i64 t = ((i64)b * L + ept - 1) / ept;
       t = (t + 31) / 32 * 32;
       return (int)std::max<i64>(t, 32);
     };
-    const size_t budget = 96 * 1024;
+    const i64 nvec = st.V;  // per column; tiles may span columns
+
+    // element-major tiles: strided input and output views whose inner
+    // extent holds whole tiles (B | Cc); rows of B * esz bytes (128 B when
+    // the thread budget allows, never below 16 B), moved by TMA boxes
+    ls.lay = 0;
+    ls.tma_in_ok = ls.tma_out_ok = 0;
+    if ((ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 && st.vout.Cc > 1) {
+      int B = 128 / esz;
+      while (B > 1 && (st.vin.Cc % B || st.vout.Cc % B)) B /= 2;
+      while (B * esz > 16 && threads_for(B) > FM_MAX_THREADS) B /= 2;
+      if (B * esz >= 16 && threads_for(B) <= FM_MAX_THREADS &&
+          st.V % B == 0) {
+        ls.lay = 1;
+        st.B = B;
+        st.Lp = L;
+        st.box_rows = std::min(L, 256);
+        st.elem_k = esz == 16 ? 2 : 1;
+        const bool rows_ok = L % st.box_rows == 0;
+        ls.tma_in_ok = rows_ok && st.in_len == st.vin.n && !st.map_in &&
+                       st.in_rows == st.vin.A * st.vin.n * st.vin.Cc;
+        ls.tma_out_ok = rows_ok && st.out_len == st.vout.n &&
+                        st.out_mode == 0 && !st.accumulate &&
+                        st.out_rows == st.vout.A * st.vout.n * st.vout.Cc;
+        ls.threads = threads_for(B);
+        int nbuf = 4;
+        while (nbuf > 2 &&
+               fmk::launch_smem(B, L, esz, nbuf) > (size_t)150 * 1024)
+          --nbuf;
+        st.nbuf = nbuf;
+        ls.smem = fmk::launch_smem(B, L, esz, nbuf);
+        if (ls.smem <= (size_t)fmk::kMaxSmem) return;
+        ls.lay = 0;  // does not fit: fall back to vector-major tiles
+        ls.tma_in_ok = ls.tma_out_ok = 0;
+      }
+    }
+
+    const int shift = esz >= 16 ? 3 : (esz == 8 ? 4 : 5);
+    int Lp = (L - 1) + ((L - 1) >> shift) + 1;
+    if ((Lp & 1) == 0) ++Lp;
+    st.Lp = Lp;
+    const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
+    int B = 1;
+    if (strided) B = std::max(1, 128 / esz);
+    const size_t budget = 110 * 1024;
+    // dynamic shared memory of a tile of b vectors: the vectors, then one
+    // addressing record and one scalar per vector
+    auto smem_for = [&](int b) { return fmk::launch_smem(b, Lp, esz, 2); };
     while (B > 1 && (threads_for(B) > FM_MAX_THREADS ||
-                     (size_t)B * Lp * P_->esz > (size_t)fmk::kMaxSmem))
+                     smem_for(B) > (size_t)fmk::kMaxSmem))
       B /= 2;
     while (threads_for(B) < 128 && threads_for(2 * B) <= FM_MAX_THREADS &&
-           (size_t)2 * B * Lp * P_->esz <= budget &&
-           (i64)B < nvec * 64)
+           smem_for(2 * B) <= budget && (i64)B < nvec * 64 && B < 1024)
       B *= 2;
     if (threads_for(B) > FM_MAX_THREADS)
       fail(FM_ERR_UNSUPPORTED, "working length too large for one tile");
     st.B = B;
     ls.threads = threads_for(B);
-    ls.smem = (size_t)B * Lp * P_->esz;
+    // deepest cp.async ring (up to 4 tiles) within ~150 KB per CTA
+    int nbuf = 4;
+    while (nbuf > 2 &&
+           fmk::launch_smem(B, Lp, esz, nbuf) > (size_t)150 * 1024)
+      --nbuf;
+    st.nbuf = nbuf;
+    ls.smem = fmk::launch_smem(B, Lp, esz, nbuf);
     if (ls.smem > (size_t)fmk::kMaxSmem)
       fail(FM_ERR_UNSUPPORTED, "tile exceeds shared memory");
   }
@@ -1164,6 +1367,115 @@ class Planner {
   }
 };
 
+// ------------------------------------------------------------ TMA descriptors
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType,
+                                  cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static std::mutex mu;
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// Describe the view (A, n, Cc) of `num_cols` columns at `base` (leading
+// dimension ld) as a 4-D tensor {Cc, n, A, columns} read in boxes of
+// {B, box_rows, 1, 1} elements.  Returns false when the buffer does not meet
+// TMA's alignment rules (the launch then uses per-thread copies).
+bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
+                 i64 ld, i64 num_cols, int B, int box_rows, int esz) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const int k = esz == 16 ? 2 : 1;
+  const int tsz = esz / k;
+  if (((uintptr_t)base & 15) || (ld * esz) % 16 || (vw.Cc * esz) % 16)
+    return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)(vw.Cc * k), (cuuint64_t)vw.n,
+                              (cuuint64_t)vw.A, (cuuint64_t)num_cols};
+  for (cuuint64_t d : dims)
+    if (d == 0 || d > (1ull << 32)) return false;
+  const cuuint64_t strides[3] = {(cuuint64_t)(vw.Cc * esz),
+                                 (cuuint64_t)(vw.n * vw.Cc * esz),
+                                 (cuuint64_t)(ld * esz)};
+  for (cuuint64_t st : strides)
+    if (st >= (1ull << 40)) return false;
+  const cuuint32_t box[4] = {(cuuint32_t)(B * k), (cuuint32_t)box_rows, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUtensorMapDataType dt =
+      tsz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_INT64;
+  return fn(tm, dt, 4, const_cast<void *>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Finish a bound launch (TMA descriptors, status word) and issue it.
+void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
+  st.err = P->err;
+  st.tma_in = st.tma_out = 0;
+  if (ls.lay == 1) {
+    if (ls.tma_in_ok && st.src_type == P->ctype) {
+      if (ls.tm_in_key != st.src || ls.tm_in_ld != st.ld_src ||
+          ls.tm_in_m != st.num_cols) {
+        ls.tm_in_key = nullptr;
+        if (encode_view(&ls.tm_in, st.src, st.vin, st.ld_src, st.num_cols,
+                        st.B, st.box_rows, P->esz)) {
+          ls.tm_in_key = st.src;
+          ls.tm_in_ld = st.ld_src;
+          ls.tm_in_m = st.num_cols;
+        }
+      }
+      if (ls.tm_in_key) {
+        st.tm_in = ls.tm_in;
+        st.tma_in = 1;
+      }
+    }
+    if (ls.tma_out_ok && st.dst_type == P->ctype) {
+      if (ls.tm_out_key != st.dst || ls.tm_out_ld != st.ld_dst ||
+          ls.tm_out_m != st.num_cols) {
+        ls.tm_out_key = nullptr;
+        if (encode_view(&ls.tm_out, st.dst, st.vout, st.ld_dst, st.num_cols,
+                        st.B, st.box_rows, P->esz)) {
+          ls.tm_out_key = st.dst;
+          ls.tm_out_ld = st.ld_dst;
+          ls.tm_out_m = st.num_cols;
+        }
+      }
+      if (ls.tm_out_key) {
+        st.tm_out = ls.tm_out;
+        st.tma_out = 1;
+      }
+    }
+  }
+  const i64 grid = (st.V * st.num_cols + st.B - 1) / st.B;
+  if (st.V * st.num_cols >= 0x7fffffffLL)
+    fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
+  cudaError_t e;
+  switch (P->ctype) {
+    case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    default: e = fmk::launch_c128(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+  }
+  CUDA_TRY(e);
+}
+
 // ------------------------------------------------------------ execution
 int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
              void *y, int y_type, i64 ld_y, i64 M, cudaStream_t s,
@@ -1190,7 +1502,7 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
   }
   size_t li = 0;
   if (events) CUDA_TRY(cudaEventRecord((*events)[li++], s));
-  for (const LStep &ls : P->steps[dir]) {
+  for (LStep &ls : P->steps[dir]) {
     fmk::Step st = ls.st;
     auto bind = [&](int id, const void *&ptr, int &type, i64 &ld) {
       if (id == 0) {
@@ -1214,17 +1526,7 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
     st.src = sp;
     st.dst = const_cast<void *>(dp);
     st.num_cols = M;
-    const i64 grid = (st.V * M + st.B - 1) / st.B;
-    if (grid > 0x7fffffffLL) fail(FM_ERR_VALUE, "too many columns");
-    cudaError_t e;
-    switch (P->ctype) {
-      case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      default: e = fmk::launch_c128(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-    }
-    CUDA_TRY(e);
+    launch_step(P, ls, st, s);
     if (events) CUDA_TRY(cudaEventRecord((*events)[li++], s));
   }
   return FM_OK;
@@ -1276,7 +1578,7 @@ int run_plan_static(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
              std::to_string((size_t)FM_STATIC_SCRATCH_BYTES) +
              "-byte static array; use fewer columns or fm_execute");
   char *base = total ? (char *)static_scratch_address() : nullptr;
-  for (const LStep &ls : P->steps[dir]) {
+  for (LStep &ls : P->steps[dir]) {
     fmk::Step st = ls.st;
     auto bind = [&](int id, const void *&ptr, int &type, i64 &ld) {
       if (id == 0) {
@@ -1300,17 +1602,7 @@ int run_plan_static(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
     st.src = sp;
     st.dst = const_cast<void *>(dp);
     st.num_cols = M;
-    const i64 grid = (st.V * M + st.B - 1) / st.B;
-    if (grid > 0x7fffffffLL) fail(FM_ERR_VALUE, "too many columns");
-    cudaError_t e;
-    switch (P->ctype) {
-      case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-      default: e = fmk::launch_c128(st, ls.cls, ls.threads, ls.smem, grid, s); break;
-    }
-    CUDA_TRY(e);
+    launch_step(P, ls, st, s);
   }
   return FM_OK;
 }
@@ -1326,6 +1618,8 @@ const char *kind_name(int k) {
     case fmk::OP_SCALE: return "scale";
     case fmk::OP_CONJ: return "conj";
     case fmk::OP_TW: return "twiddle";
+    case fmk::OP_DIF: return "fft-dif";
+    case fmk::OP_DIT: return "fft-dit";
   }
   return "?";
 }
@@ -1386,6 +1680,9 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
     P->rows = nodes[root].rows;
     P->cols = nodes[root].cols;
     Planner(P.get(), recs).build(root);
+    CUDA_TRY(cudaMalloc(&P->err, sizeof(int)));
+    P->allocs.push_back(P->err);
+    CUDA_TRY(cudaMemset(P->err, 0, sizeof(int)));
     CUDA_TRY(cudaDeviceSynchronize());
     *out_plan = P.release();
     return FM_OK;
@@ -1502,6 +1799,22 @@ int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
     CUDA_TRY(cudaMemcpyAsync(y, plan->dy, by, cudaMemcpyDeviceToHost,
                              plan->hstream));
     CUDA_TRY(cudaStreamSynchronize(plan->hstream));
+    return fm_plan_check(plan);
+  });
+}
+
+int fm_plan_check(fm_plan *plan) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (!plan->err) return FM_OK;
+    int e = 0;
+    CUDA_TRY(cudaMemcpy(&e, plan->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e != 0) {
+      CUDA_TRY(cudaMemset(plan->err, 0, sizeof(int)));
+      fail(FM_ERR_TIMEOUT,
+           "a bounded wait for a tile copy gave up; results of the affected "
+           "call are incomplete");
+    }
     return FM_OK;
   });
 }
@@ -1555,6 +1868,7 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
       if (st.map_in) s += " map_in";
       if (st.pre) s += " pre";
       if (st.post) s += " post";
+      if (st.out_pos) s += " out_perm";
       s += "\n";
     }
     const size_t n = std::min<size_t>(s.size(), (size_t)buf_len - 1);

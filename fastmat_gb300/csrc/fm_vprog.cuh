@@ -13,6 +13,8 @@
 // and writes HBM once.
 #pragma once
 
+#include <cuda.h>
+
 #include "fm_types.cuh"
 
 namespace fmk {
@@ -26,7 +28,10 @@ enum OpKind {
   OP_DENSE = 6,   // v'[i] = sum_j M[i + j * len] v[j], i < len, j < len2
   OP_SCALE = 7,   // v[j] *= (sre + i sim), j < len
   OP_CONJ = 8,    // v[j] = conj(v[j]), j < len
-  OP_TW = 9       // v[j] *= exp(sign 2 pi i ((q * j) mod N) / N), j < len
+  OP_TW = 9,      // v[j] *= exp(sign 2 pi i ((q * nat(j)) mod N) / N),
+                  // nat = perm table (ptr2) or identity, j < len
+  OP_DIF = 10,    // in-place FFT, natural order in, digit-reversed out
+  OP_DIT = 11     // in-place FFT, digit-reversed in, natural order out
 };
 
 #define FM_MAX_OPS 14
@@ -39,6 +44,7 @@ struct Op {
   int nrad;
   unsigned char rad[16];  // FFT radices / FWHT bit-group widths
   const void *ptr;        // twiddles, vector, map, matrix
+  const int *ptr2;        // TW: storage position -> natural index
   i64 div, mod, stride;   // q = (v / div) % mod for MUL / TW
   i64 N;
   double sre, sim;
@@ -49,6 +55,10 @@ struct View {
 };
 
 struct Step {
+  // TMA descriptors of the input / output views (element-major tiles only;
+  // encoded on the host per call because they hold the buffer address)
+  alignas(64) CUtensorMap tm_in;
+  alignas(64) CUtensorMap tm_out;
   const void *src;
   void *dst;
   i64 ld_src, ld_dst;
@@ -62,9 +72,15 @@ struct Step {
   int n_out;     // gather mode: rows written per column
   const void *pre;
   const void *post;
+  const int *out_pos;  // storer: natural element j sits at position out_pos[j]
+  int *err;            // device status word (bounded waits that gave up)
   int conj_in, conj_out, accumulate, has_scale;
   double scale_re, scale_im;
   int L, Lp, B;
+  int nbuf;      // tile buffers of the copy ring (2..4)
+  int tma_in, tma_out;  // element-major tiles moved by TMA boxes
+  int box_rows;  // rows per TMA box (<= 256)
+  int elem_k;    // TMA elements per E (2 for 16-byte E)
   int in_len, out_len;
   i64 V;         // vectors per column
   i64 num_cols;
@@ -78,7 +94,7 @@ struct Step {
 // FM_MAX_THREADS * Ept elements)
 #define FM_MAX_THREADS 512
 template <class E> struct Ept {
-  static constexpr int v = sizeof(E) >= 16 ? 8 : 16;
+  static constexpr int v = sizeof(E) == 4 ? 16 : 8;
 };
 
 // ------------------------------------------------------------ small DFTs
@@ -253,97 +269,277 @@ template <int R, class C> __device__ __forceinline__ void dft(C *v, int sign) {
   else if constexpr (R == 16) dft16(v, sign);
 }
 
-// ------------------------------------------------------------ FFT pass
-// One Stockham autosort pass of radix R over all B vectors of the tile
-// (decimation in time; output of the last pass is in natural order).
-template <int R, class C>
-__device__ __forceinline__ void fft_pass(C *sm, int Lp, int B, int Lf, int Ns,
-                                         int sign, const C *__restrict__ tw,
-                                         int tid, int T) {
-  // odd radices hold half as many elements per thread (the planner gives
-  // programs with odd radices twice the threads)
-  constexpr int EP = (R & 1) ? Ept<C>::v / 2 : Ept<C>::v;
-  constexpr int MB = (EP + R - 1) / R;
-  const int nb = Lf / R;
-  const int total = B * nb;
-  C v[MB][R];
+// ------------------------------------------------------------ in-place pow2 DFT
+// Decimation-in-frequency radix-2 network over R registers, in place: after
+// it, v[i] holds output bitrev(i).  Twiddles are compile-time constants
+// exp(sign 2 pi i k / M), taken from cos/sin of multiples of pi / 8.
+__host__ __device__ constexpr double kCos16(int i) {
+  // cos(2 pi i / 16), i = 0..15
+  return i == 0 ? 1.0 : i == 1 ? 0.9238795325112867 : i == 2 ? 0.7071067811865476
+       : i == 3 ? 0.3826834323650898 : i == 4 ? 0.0 : i == 5 ? -0.3826834323650898
+       : i == 6 ? -0.7071067811865476 : i == 7 ? -0.9238795325112867
+       : i == 8 ? -1.0 : i == 9 ? -0.9238795325112867 : i == 10 ? -0.7071067811865476
+       : i == 11 ? -0.3826834323650898 : i == 12 ? 0.0 : i == 13 ? 0.3826834323650898
+       : i == 14 ? 0.7071067811865476 : 0.9238795325112867;
+}
+__host__ __device__ constexpr double kSin16(int i) { return kCos16((i + 12) & 15); }
+
+template <int M, int K, class C>
+__device__ __forceinline__ C twc(C x, int sign) {
+  typedef typename Tr<C>::R R;
+  constexpr int idx = (16 / M) * K;  // angle 2 pi idx / 16
+  if constexpr (idx == 0) {
+    return x;
+  } else if constexpr (idx == 4) {
+    return rot90(x, sign);  // * (i sign)
+  } else {
+    const R c = (R)kCos16(idx), sn = (R)(sign * kSin16(idx));
+    C r;
+    r.x = x.x * c - x.y * sn;
+    r.y = x.x * sn + x.y * c;
+    return r;
+  }
+}
+
+template <int R, int H, int K, class C>
+__device__ __forceinline__ void dif_stage_k(C *v, int sign) {
+  if constexpr (K < H) {
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int g = tid + i * T;
-    if (g < total) {
-      const int b = g / nb, q = g - b * nb;
-      const C *vec = sm + b * Lp;
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[i][r] = vec[pidx<C>(q + r * nb)];
+    for (int blk = 0; blk < R; blk += 2 * H) {
+      const C a = v[blk + K], b = v[blk + K + H];
+      v[blk + K] = a + b;
+      v[blk + K + H] = twc<2 * H, K>(a - b, sign);
+    }
+    dif_stage_k<R, H, K + 1>(v, sign);
+  }
+}
+
+template <int R, int H, class C>
+__device__ __forceinline__ void dif_stages(C *v, int sign) {
+  if constexpr (H >= 1) {
+    dif_stage_k<R, H, 0>(v, sign);
+    dif_stages<R, H / 2>(v, sign);
+  }
+}
+
+template <int R> __host__ __device__ constexpr int brev(int i) {
+  int r = 0;
+  for (int b = 1; b < R; b <<= 1) r = (r << 1) | ((i & b) ? 1 : 0);
+  return r;
+}
+
+// ------------------------------------------------------------ index helpers
+// Unsigned division by a runtime divisor 1 <= d < 2^31 for dividends below
+// 2^31 with one multiply-high: q = (umulhi(n, m) + n) >> s,
+// s = ceil(log2 d), m = 2^32 (2^s - d) / d + 1 (round-up multiplier).
+struct FDiv {
+  unsigned d, m, s;
+  __device__ __forceinline__ explicit FDiv(unsigned d_) : d(d_), s(0) {
+    while ((1u << s) < d) ++s;
+    m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  }
+  __device__ __forceinline__ unsigned div(unsigned n) const {
+    return (__umulhi(n, m) + n) >> s;
+  }
+};
+
+// Walks the flat index f = tid, tid + T, ... of a tile of vectors of length
+// len, keeping (b, j) = (f / len, f % len) without dividing per step.
+struct Walk {
+  int b, j, tb, tj, len;
+  __device__ __forceinline__ Walk(int f0, int len_, int T) : len(len_) {
+    b = f0 / len;
+    j = f0 - b * len;
+    tb = T / len;
+    tj = T - tb * len;
+  }
+  __device__ __forceinline__ void next() {
+    j += tj;
+    b += tb;
+    if (j >= len) {
+      j -= len;
+      ++b;
     }
   }
-  __syncthreads();
-  const int tstep = Lf / (Ns * R);
+};
+
+// Per-vector addressing of a tile, computed once per launch: column offsets
+// of source and destination, the row of element 0 in the input and output
+// views (-1: vector beyond the operand) and the vector's index within its
+// column.
+struct VInfo {
+  i64 col_src, rb_in, col_dst, rb_out, vcol;
+};
+
+// ------------------------------------------------------------ layouts
+// LAY 0: vector-major tile, vector b at b * Lp with one pad element per 128
+//        bytes (pidx), threads walk the elements of a vector.
+// LAY 1: element-major tile, element j of vector b at j * B + b (dense),
+//        threads walk the vectors first; filled and drained by TMA boxes.
+template <class E, int LAY>
+__device__ __forceinline__ int jx(int j, int B) {
+  if constexpr (LAY == 1) return j * B;
+  else return pidx<E>(j);
+}
+template <class E, int LAY>
+__device__ __forceinline__ E *vbase(E *sm, int b, int Lp) {
+  if constexpr (LAY == 1) return sm + b;
+  else return sm + b * Lp;
+}
+
+// ------------------------------------------------------------ FFT stages
+// In-place mixed-radix stages.  With L = R_1 ... R_S and M_0 = L,
+// M_s = M_{s-1} / R_s, stage s of the DIF transform takes, for every block
+// K (offset K M_{s-1}) and t < M_s, the R_s elements at K M_{s-1} + t + M_s n,
+// applies the radix-R_s DFT over n, multiplies output k by
+// w_{M_{s-1}}^{t k} and writes it back to K M_{s-1} + t + M_s k.  After all
+// stages position ((k_1 R_2 + k_2) R_3 + ...) holds output
+// k_1 + R_1 (k_2 + R_2 (...)).  The DIT transform runs the stages in reverse
+// (twiddle first, then the DFT over k), taking that digit-reversed order to
+// natural order; with opposite signs the two are inverse up to the factor L.
+// Each work item reads and writes the same R positions, so a stage needs one
+// barrier and holds only R values per thread.
+template <int R, bool DIT, int LAY, class C>
+__device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
+                                          int Mprev, int sign,
+                                          const C *__restrict__ tw, int tid,
+                                          int T) {
+  const int M = Mprev / R;
+  const int nw = Lf / R;
+  const int total = B * nw;
+  const FDiv dnw((unsigned)nw), dM((unsigned)M);
+  const int lgB = __ffs(B) - 1;
+  const int tscale = Lf / Mprev;
+  for (int g = tid; g < total; g += T) {
+    int b, w;
+    if constexpr (LAY == 1) {
+      b = g & (B - 1);
+      w = g >> lgB;
+    } else {
+      b = (int)dnw.div((unsigned)g);
+      w = g - b * nw;
+    }
+    const int K = (int)dM.div((unsigned)w), t = w - K * M;
+    C *vec = vbase<C, LAY>(sm, b, Lp);
+    const int base = K * Mprev + t;
+    C v[R];
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int g = tid + i * T;
-    if (g < total) {
-      const int b = g / nb, q = g - b * nb;
-      const int k = q % Ns;
-      if (Ns > 1) {
+    for (int n = 0; n < R; ++n) v[n] = vec[jx<C, LAY>(base + M * n, B)];
+    if constexpr (DIT) {
+      if (t != 0) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) {
-          const C w = tw[r * k * tstep];
-          v[i][r] = sign < 0 ? cmul(v[i][r], w) : cmulc(v[i][r], w);
+        for (int k = 1; k < R; ++k) {
+          const C w = tw[t * k * tscale];
+          v[k] = sign < 0 ? cmul(v[k], w) : cmulc(v[k], w);
         }
       }
-      dft<R>(v[i], sign);
-      C *vec = sm + b * Lp;
-      const int base = (q - k) * R + k;
+    }
+    if constexpr ((R & (R - 1)) == 0) {
+      dif_stages<R, R / 2>(v, sign);  // v[i] = output brev(i)
 #pragma unroll
-      for (int r = 0; r < R; ++r) vec[pidx<C>(base + r * Ns)] = v[i][r];
+      for (int i = 0; i < R; ++i) {
+        C y = v[i];
+        if constexpr (!DIT) {
+          if (t != 0 && brev<R>(i) != 0) {
+            const C w = tw[t * brev<R>(i) * tscale];
+            y = sign < 0 ? cmul(y, w) : cmulc(y, w);
+          }
+        }
+        vec[jx<C, LAY>(base + M * brev<R>(i), B)] = y;
+      }
+    } else {
+      dft<R>(v, sign);
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        C y = v[k];
+        if constexpr (!DIT) {
+          if (t != 0 && k != 0) {
+            const C w = tw[t * k * tscale];
+            y = sign < 0 ? cmul(y, w) : cmulc(y, w);
+          }
+        }
+        vec[jx<C, LAY>(base + M * k, B)] = y;
+      }
     }
   }
   __syncthreads();
 }
 
-template <class C, int CLS>
+template <bool DIT, int CLS, int LAY, class C>
+__device__ __forceinline__ void fft_stage_r(int R, C *sm, int Lp, int B,
+                                            int Lf, int Mprev, int sign,
+                                            const C *tw, int tid, int T) {
+  switch (R) {
+    case 2: fft_stage<2, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
+    case 4: fft_stage<4, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
+    case 8: fft_stage<8, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
+    case 16: fft_stage<16, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
+    case 3:
+      if constexpr (CLS != 1)
+        fft_stage<3, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
+      break;
+    case 5:
+      if constexpr (CLS != 1)
+        fft_stage<5, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
+      break;
+    case 7:
+      if constexpr (CLS != 1)
+        fft_stage<7, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
+      break;
+    default: break;
+  }
+}
+
+template <class C, int CLS, int LAY>
 __device__ void run_fft(const Op &op, C *sm, int Lp, int B, int tid, int T) {
   const C *tw = (const C *)op.ptr;
-  int Ns = 1;
-  for (int p = 0; p < op.nrad; ++p) {
-    const int R = op.rad[p];
-    switch (R) {
-      case 2: fft_pass<2>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      case 3: if constexpr (CLS != 1) fft_pass<3>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      case 4: fft_pass<4>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      case 5: if constexpr (CLS != 1) fft_pass<5>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      case 7: if constexpr (CLS != 1) fft_pass<7>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      case 8: fft_pass<8>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T); break;
-      default:
-        if constexpr (Ept<C>::v >= 16)
-          fft_pass<16>(sm, Lp, B, op.len, Ns, op.sign, tw, tid, T);
-        break;
+  if (op.kind == OP_DIF) {
+    int Mprev = op.len;
+    for (int p = 0; p < op.nrad; ++p) {
+      const int R = op.rad[p];
+      fft_stage_r<false, CLS, LAY>(R, sm, Lp, B, op.len, Mprev, op.sign, tw,
+                                   tid, T);
+      Mprev /= R;
     }
-    Ns *= R;
+  } else {
+    int Mprev = 1;
+    for (int p = op.nrad - 1; p >= 0; --p) {
+      Mprev *= op.rad[p];
+      fft_stage_r<true, CLS, LAY>(op.rad[p], sm, Lp, B, op.len, Mprev,
+                                  op.sign, tw, tid, T);
+    }
   }
 }
 
 // ------------------------------------------------------------ FWHT pass
 // In-place butterflies over the bit group [s, s + K) of every element index.
-template <int K, class E>
+template <int K, int LAY, class E>
 __device__ __forceinline__ void fwht_pass(E *sm, int Lp, int B, int Lf, int s,
                                           int tid, int T) {
   constexpr int R = 1 << K;
   constexpr int MB = (Ept<E>::v + R - 1) / R;
   const int nb = Lf >> K;
+  const int lg = __ffs(nb) - 1;
+  const int lgB = __ffs(B) - 1;
   const int total = B * nb;
   const int lomask = (1 << s) - 1;
 #pragma unroll
   for (int i = 0; i < MB; ++i) {
     const int g = tid + i * T;
     if (g < total) {
-      const int b = g / nb, q = g - b * nb;
+      int b, q;
+      if constexpr (LAY == 1) {
+        b = g & (B - 1);
+        q = g >> lgB;
+      } else {
+        b = g >> lg;
+        q = g & (nb - 1);
+      }
       const int base = ((q >> s) << (s + K)) | (q & lomask);
-      E *vec = sm + b * Lp;
+      E *vec = vbase<E, LAY>(sm, b, Lp);
       E v[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = vec[pidx<E>(base + (r << s))];
+      for (int r = 0; r < R; ++r) v[r] = vec[jx<E, LAY>(base + (r << s), B)];
 #pragma unroll
       for (int h = 1; h < R; h <<= 1) {
 #pragma unroll
@@ -356,30 +552,29 @@ __device__ __forceinline__ void fwht_pass(E *sm, int Lp, int B, int Lf, int s,
         }
       }
 #pragma unroll
-      for (int r = 0; r < R; ++r) vec[pidx<E>(base + (r << s))] = v[r];
+      for (int r = 0; r < R; ++r) vec[jx<E, LAY>(base + (r << s), B)] = v[r];
     }
   }
   __syncthreads();
 }
 
-template <class E>
+template <class E, int LAY>
 __device__ void run_fwht(const Op &op, E *sm, int Lp, int B, int tid, int T) {
   int s = 0;
   for (int p = 0; p < op.nrad; ++p) {
     const int K = op.rad[p];
     switch (K) {
-      case 1: fwht_pass<1>(sm, Lp, B, op.len, s, tid, T); break;
-      case 2: fwht_pass<2>(sm, Lp, B, op.len, s, tid, T); break;
-      case 3: fwht_pass<3>(sm, Lp, B, op.len, s, tid, T); break;
-      default:
-        if constexpr (Ept<E>::v >= 16) fwht_pass<4>(sm, Lp, B, op.len, s, tid, T);
-        break;
+      case 1: fwht_pass<1, LAY>(sm, Lp, B, op.len, s, tid, T); break;
+      case 2: fwht_pass<2, LAY>(sm, Lp, B, op.len, s, tid, T); break;
+      case 3: fwht_pass<3, LAY>(sm, Lp, B, op.len, s, tid, T); break;
+      default: fwht_pass<4, LAY>(sm, Lp, B, op.len, s, tid, T); break;
     }
     s += K;
   }
 }
 
 // ------------------------------------------------------------ other ops
+// (gathers and dense products run on vector-major tiles only)
 template <class E>
 __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
                            int T) {
@@ -387,23 +582,22 @@ __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
   const i64 *map = (const i64 *)op.ptr;
   const int total = B * op.len;
   E v[MB];
+  {
+    Walk w(tid, op.len, T);
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int f = tid + i * T;
-    if (f < total) {
-      const int b = f / op.len, j = f - b * op.len;
-      const i64 src = map[j];
-      v[i] = src < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)src)];
+    for (int i = 0; i < MB; ++i, w.next()) {
+      if (tid + i * T < total) {
+        const i64 src = map[w.j];
+        v[i] = src < 0 ? zero<E>() : sm[w.b * Lp + pidx<E>((int)src)];
+      }
     }
   }
   __syncthreads();
+  {
+    Walk w(tid, op.len, T);
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int f = tid + i * T;
-    if (f < total) {
-      const int b = f / op.len, j = f - b * op.len;
-      sm[b * Lp + pidx<E>(j)] = v[i];
-    }
+    for (int i = 0; i < MB; ++i, w.next())
+      if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
   }
   __syncthreads();
 }
@@ -416,43 +610,55 @@ __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
   const int rows = op.len, cols = op.len2;
   const int total = B * rows;
   E v[MB];
+  {
+    Walk w(tid, rows, T);
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int f = tid + i * T;
-    if (f < total) {
-      const int b = f / rows, r = f - b * rows;
-      const E *vec = sm + b * Lp;
-      E acc = zero<E>();
-      for (int j = 0; j < cols; ++j)
-        acc = addv(acc, mulv(M[r + (i64)j * rows], vec[pidx<E>(j)], false));
-      v[i] = acc;
+    for (int i = 0; i < MB; ++i, w.next()) {
+      if (tid + i * T < total) {
+        const E *vec = sm + w.b * Lp;
+        E acc = zero<E>();
+        for (int j = 0; j < cols; ++j)
+          acc = addv(acc, mulv(M[w.j + (i64)j * rows], vec[pidx<E>(j)],
+                               false));
+        v[i] = acc;
+      }
     }
   }
   __syncthreads();
+  {
+    Walk w(tid, rows, T);
 #pragma unroll
-  for (int i = 0; i < MB; ++i) {
-    const int f = tid + i * T;
-    if (f < total) {
-      const int b = f / rows, r = f - b * rows;
-      sm[b * Lp + pidx<E>(r)] = v[i];
-    }
+    for (int i = 0; i < MB; ++i, w.next())
+      if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
   }
   __syncthreads();
 }
 
-template <class E>
-__device__ void run_elementwise(const Op &op, E *sm, int Lp, int B, i64 gv0,
-                                i64 V, int tid, int T) {
+template <class E, int LAY>
+__device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
+                                const VInfo *vi, i64 *sq, int tid, int T) {
+  const bool per_vec = op.kind == OP_MUL || op.kind == OP_TW;
+  if (per_vec) {
+    for (int b = tid; b < B; b += T) sq[b] = (vi[b].vcol / op.div) % op.mod;
+    __syncthreads();
+  }
   const int len = op.len;
   const int total = B * len;
-  for (int f = tid; f < total; f += T) {
-    const int b = f / len, j = f - b * len;
-    E *e = sm + b * Lp + pidx<E>(j);
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, len, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if constexpr (LAY == 1) {
+      b = f & (B - 1);
+      j = f >> lgB;
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    E *e = vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B);
     switch (op.kind) {
       case OP_MUL: {
-        const i64 v = (gv0 + b) % V;
-        const i64 q = (v / op.div) % op.mod;
-        const E m = ((const E *)op.ptr)[q * op.stride + j];
+        const E m = ((const E *)op.ptr)[sq[b] * op.stride + j];
         *e = mulv(*e, m, op.sign != 0);
         break;
       }
@@ -460,11 +666,10 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B, i64 gv0,
       case OP_CONJ: *e = conjv(*e); break;
       case OP_TW: {
         if constexpr (Tr<E>::cplx) {
-          const i64 v = (gv0 + b) % V;
-          const i64 q = (v / op.div) % op.mod;
-          const i64 t = (q * (i64)j) % op.N;
-          const E w = ((const E *)op.ptr)[t];
-          *e = op.sign < 0 ? cmul(*e, w) : cmulc(*e, w);
+          const int nat = op.ptr2 ? op.ptr2[j] : j;
+          const i64 t = (sq[b] * (i64)nat) % op.N;
+          const E wv = ((const E *)op.ptr)[t];
+          *e = op.sign < 0 ? cmul(*e, wv) : cmulc(*e, wv);
         }
         break;
       }
@@ -474,129 +679,578 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B, i64 gv0,
   __syncthreads();
 }
 
-template <class E>
+template <class E, int LAY>
 __device__ void run_zpad(const Op &op, E *sm, int Lp, int B, int tid, int T) {
   const int cnt = op.len2 - op.len;
   const int total = B * cnt;
-  for (int f = tid; f < total; f += T) {
-    const int b = f / cnt, j = op.len + (f - b * cnt);
-    sm[b * Lp + pidx<E>(j)] = zero<E>();
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, cnt, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if constexpr (LAY == 1) {
+      b = f & (B - 1);
+      j = f >> lgB;
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    vbase<E, LAY>(sm, b, Lp)[jx<E, LAY>(op.len + j, B)] = zero<E>();
   }
   __syncthreads();
 }
+
+// ------------------------------------------------------------ async copies
+// cp.async: per-thread global -> shared copies that complete in the
+// background; src_bytes = 0 writes zeros without reading global memory.
+template <int N>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem,
+                                         bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? N : 0;
+  if constexpr (N == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s),
+                 "l"(gmem), "r"(n));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s),
+                 "l"(gmem), "n"(N), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::);
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+// wait until at most n groups are pending (n = 0..3)
+__device__ __forceinline__ void cp_async_wait_n(int n) {
+  switch (n) {
+    case 0: cp_async_wait<0>(); break;
+    case 1: cp_async_wait<1>(); break;
+    case 2: cp_async_wait<2>(); break;
+    default: cp_async_wait<3>(); break;
+  }
+}
+
+// ---- TMA (cp.async.bulk.tensor) with mbarrier completion
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return done != 0;
+}
+// bounded wait: gives up after `limit` polls (each poll may suspend the
+// thread for a while) and reports false
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned phase,
+                                          long long limit) {
+  for (long long it = 0; it < limit; ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *tm,
+                                            int c0, int c1, int c2, int c3,
+                                            unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::"
+      "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(dst),
+      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap *tm,
+                                             unsigned src, int c0, int c1,
+                                             int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group "
+      "[%0, {%1, %2, %3, %4}], [%5];\n" ::"l"(tm),
+      "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(src)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// bytes of one tile buffer (B vectors of Lp elements), 128-byte aligned
+__host__ __device__ __forceinline__ size_t tile_bytes(int B, int Lp,
+                                                      int esz) {
+  return ((size_t)B * Lp * esz + 127) / 128 * 128;
+}
+
+// dynamic shared memory of a launch: nbuf tile buffers, nbuf mbarriers,
+// nbuf sets of per-vector records and one per-vector scalar array
+__host__ __device__ __forceinline__ size_t launch_smem(int B, int Lp, int esz,
+                                                       int nbuf) {
+  return nbuf * tile_bytes(B, Lp, esz) + 8 * (size_t)nbuf +
+         (size_t)B * (nbuf * sizeof(VInfo) + 8);
+}
+
+// per-vector addressing of tile `tile` (vector indices below 2^31)
+__device__ __forceinline__ void setup_tile(const Step &p, VInfo *vi,
+                                           i64 tile, const FDiv &dV,
+                                           const FDiv &dci, const FDiv &dco,
+                                           i64 nvec, int tid, int T) {
+  for (int b = tid; b < p.B; b += T) {
+    const i64 gv = tile * p.B + b;
+    VInfo x;
+    if (gv < nvec) {
+      const unsigned g = (unsigned)gv;
+      const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
+      const unsigned a = dci.div(v), c = v - a * (unsigned)p.vin.Cc;
+      const unsigned a2 = dco.div(v), c2 = v - a2 * (unsigned)p.vout.Cc;
+      x.col_src = (i64)m * p.ld_src;
+      x.rb_in = (i64)a * p.vin.n * p.vin.Cc + c;
+      x.col_dst = (i64)m * p.ld_dst;
+      x.rb_out = (i64)a2 * p.vout.n * p.vout.Cc + c2;
+      x.vcol = v;
+    } else {
+      x.col_src = x.col_dst = x.vcol = 0;
+      x.rb_in = x.rb_out = -1;
+    }
+    vi[b] = x;
+  }
+}
+
+// TMA coordinates of an element-major tile: all B vectors share column m and
+// outer index a (the planner makes B divide Cc), inner offset c0.
+__device__ __forceinline__ void tile_coords(const Step &p, i64 tile,
+                                            const View &vw, int &c0, int &a,
+                                            int &m) {
+  const i64 gv = tile * p.B;
+  const i64 mm = gv / p.V, v = gv - mm * p.V;
+  const i64 aa = v / vw.Cc;
+  c0 = (int)(v - aa * vw.Cc);
+  a = (int)aa;
+  m = (int)mm;
+}
+
+template <class E>
+__device__ __forceinline__ void tma_issue_load(const Step &p, E *sm,
+                                               unsigned bar, i64 tile) {
+  int c0, a, m;
+  tile_coords(p, tile, p.vin, c0, a, m);
+  const unsigned bytes = (unsigned)((size_t)p.B * p.L * sizeof(E));
+  mbar_expect_tx(bar, bytes);
+  for (int j0 = 0; j0 < p.L; j0 += p.box_rows)
+    tma_load_4d(smem_addr(sm + (size_t)j0 * p.B), &p.tm_in, c0 * p.elem_k,
+                j0, a, m, bar);
+}
+
+template <class E>
+__device__ __forceinline__ void tma_issue_store(const Step &p, const E *sm,
+                                                i64 tile) {
+  int c0, a, m;
+  tile_coords(p, tile, p.vout, c0, a, m);
+  fence_async_smem();
+  for (int j0 = 0; j0 < p.out_len; j0 += p.box_rows)
+    tma_store_4d(&p.tm_out, smem_addr(sm + (size_t)j0 * p.B), c0 * p.elem_k,
+                 j0, a, m);
+  bulk_commit();
+}
+
+// asynchronous per-thread load of a tile whose source already has the
+// compute type and needs no gather: every element (zero padding included)
+// is one cp.async
+template <class E, int LAY>
+__device__ __forceinline__ void load_async(const Step &p, E *sm,
+                                           const VInfo *vi, int tid, int T) {
+  const int B = p.B, L = p.L, Lp = p.Lp;
+  const int total = B * L;
+  const E *src = (const E *)p.src;
+  const i64 cc = p.vin.Cc;
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, L, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if (cc > 1 || LAY == 1) {
+      j = f >> lgB;
+      b = f & (B - 1);
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    const i64 rb = vi[b].rb_in;
+    const i64 r = rb + (i64)j * cc;
+    const bool ok = rb >= 0 && j < p.in_len && r < p.in_rows;
+    cp_async<sizeof(E)>(vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B),
+                        ok ? (const void *)(src + vi[b].col_src + r)
+                           : (const void *)src,
+                        ok);
+  }
+}
+
+// synchronous load with type conversion, gather map, conjugation and
+// pre-multiplication
+template <class E, int LAY>
+__device__ __forceinline__ void load_general(const Step &p, E *sm,
+                                             const VInfo *vi, int tid,
+                                             int T) {
+  const int B = p.B, L = p.L, Lp = p.Lp;
+  const int total = B * L;
+  const i64 cc = p.vin.Cc;
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, L, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if (cc > 1 || LAY == 1) {
+      j = f >> lgB;
+      b = f & (B - 1);
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    E val = zero<E>();
+    const i64 rb = vi[b].rb_in;
+    if (rb >= 0 && j < p.in_len) {
+      const i64 r = rb + (i64)j * cc;
+      if (r < p.in_rows) {
+        const i64 srow = p.map_in ? p.map_in[r] : r;
+        if (srow >= 0) {
+          val = load_as<E>(p.src, p.src_type, vi[b].col_src + srow);
+          if (p.conj_in) val = conjv(val);
+          if (p.pre) val = mulv(val, ((const E *)p.pre)[r], false);
+        }
+      }
+    }
+    vbase<E, LAY>(sm, b, Lp)[jx<E, LAY>(j, B)] = val;
+  }
+}
+
+// conjugation / pre-multiplication applied in shared memory after an
+// asynchronous load
+template <class E, int LAY>
+__device__ __forceinline__ void load_fixup(const Step &p, E *sm,
+                                           const VInfo *vi, int tid, int T) {
+  const int B = p.B, L = p.L, Lp = p.Lp;
+  const int total = B * L;
+  const i64 cc = p.vin.Cc;
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, L, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if constexpr (LAY == 1) {
+      b = f & (B - 1);
+      j = f >> lgB;
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    const i64 rb = vi[b].rb_in;
+    if (rb < 0 || j >= p.in_len) continue;
+    const i64 r = rb + (i64)j * cc;
+    if (r >= p.in_rows) continue;
+    E *e = vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B);
+    E val = *e;
+    if (p.conj_in) val = conjv(val);
+    if (p.pre) val = mulv(val, ((const E *)p.pre)[r], false);
+    *e = val;
+  }
+}
+
+// element-major tiles before a TMA store: reorder (out_pos), post-multiply,
+// scale and conjugate in shared memory
+template <class E>
+__device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
+                                               const VInfo *vi, int tid,
+                                               int T) {
+  const int B = p.B;
+  const int total = B * p.out_len;
+  const int lgB = __ffs(B) - 1;
+  const i64 cc = p.vout.Cc;
+  if (p.out_pos) {
+    // permute through registers: gather, barrier, write back
+    constexpr int MB = Ept<E>::v;
+    E v[MB];
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int f = tid + i * T;
+      if (f < total)
+        v[i] = sm[p.out_pos[f >> lgB] * B + (f & (B - 1))];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < MB; ++i) {
+      const int f = tid + i * T;
+      if (f < total) sm[f] = v[i];
+    }
+    __syncthreads();
+  }
+  if (!p.post && !p.has_scale && !p.conj_out) return;
+  for (int f = tid; f < total; f += T) {
+    const int b = f & (B - 1), j = f >> lgB;
+    E val = sm[f];
+    if (p.post) {
+      const i64 rb = vi[b].rb_out;
+      if (rb >= 0) val = mulv(val, ((const E *)p.post)[rb + (i64)j * cc], false);
+    }
+    if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+    if (p.conj_out) val = conjv(val);
+    sm[f] = val;
+  }
+  __syncthreads();
+}
+
+template <class E, int LAY>
+__device__ __forceinline__ void store_tile(const Step &p, const E *sm,
+                                           const VInfo *vi, int tid, int T) {
+  const int B = p.B, Lp = p.Lp;
+  const bool acc = p.accumulate != 0;
+  if constexpr (LAY == 0) {
+    if (p.out_mode == 1) {
+      // gather: out row i of column m takes vector element map_out[i]
+      Walk w(tid, p.n_out, T);
+      for (int f = tid; f < B * p.n_out; f += T, w.next()) {
+        const int b = w.b, i = w.j;
+        if (vi[b].rb_out < 0) continue;
+        const i64 j = p.map_out[i];
+        E val = j < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)j)];
+        if (j >= 0 && p.post) val = mulv(val, ((const E *)p.post)[j], false);
+        if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+        if (p.conj_out) val = conjv(val);
+        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + i, val, acc);
+      }
+      return;
+    }
+  }
+  const i64 ccout = p.vout.Cc;
+  const int total = B * p.out_len;
+  const int lgB = __ffs(B) - 1;
+  Walk w(tid, p.out_len, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if (ccout > 1 || LAY == 1) {
+      j = f >> lgB;
+      b = f & (B - 1);
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    const i64 rb = vi[b].rb_out;
+    if (rb < 0) continue;
+    const i64 r = rb + (i64)j * ccout;
+    if (r >= p.out_rows) continue;
+    const i64 drow = p.out_mode == 2 ? p.map_out[r] : r;
+    if (drow < 0) continue;
+    E val = vbase<E, LAY>(const_cast<E *>(sm), b, Lp)
+        [jx<E, LAY>(p.out_pos ? p.out_pos[j] : j, B)];
+    if (p.post) val = mulv(val, ((const E *)p.post)[r], false);
+    if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+    if (p.conj_out) val = conjv(val);
+    if (p.dst_type == Tr<E>::code && !acc)
+      ((E *)p.dst)[vi[b].col_dst + drow] = val;
+    else
+      store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc);
+  }
+}
+
+template <class E, int CLS, int LAY>
+__device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
+                                            int B, const VInfo *vi, i64 *sq,
+                                            int tid, int T) {
+  for (int o = 0; o < p.nops; ++o) {
+    const Op &op = p.ops[o];
+    switch (op.kind) {
+      case OP_DIF:
+      case OP_DIT:
+        if constexpr (Tr<E>::cplx && CLS != 3)
+          run_fft<E, CLS, LAY>(op, sm, Lp, B, tid, T);
+        break;
+      case OP_FWHT:
+        if constexpr (CLS == 0 || CLS == 3)
+          run_fwht<E, LAY>(op, sm, Lp, B, tid, T);
+        break;
+      case OP_GATHER:
+        if constexpr (CLS == 0 && LAY == 0)
+          run_gather<E>(op, sm, Lp, B, tid, T);
+        break;
+      case OP_DENSE:
+        if constexpr (CLS == 0 && LAY == 0)
+          run_dense<E>(op, sm, Lp, B, tid, T);
+        break;
+      case OP_ZPAD: run_zpad<E, LAY>(op, sm, Lp, B, tid, T); break;
+      default:
+        run_elementwise<E, LAY>(op, sm, Lp, B, vi, sq, tid, T);
+        break;
+    }
+  }
+}
+
+// polls of a bounded mbarrier wait before a launch reports FM_ERR_TIMEOUT
+#define FM_WAIT_LIMIT (1LL << 22)
 
 // ------------------------------------------------------------ the kernel
 // CLS selects the op subset compiled into an instantiation, so the hot
 // programs (power-of-two FFT, FWHT) do not carry the register pressure of
 // the rarely used ops: 1 = pow2 FFT + pointwise, 2 = FFT with radices 3/5/7,
-// 3 = FWHT + pointwise, 0 = everything.
-template <class E, int CLS>
-__global__ void __launch_bounds__(FM_MAX_THREADS)
+// 3 = FWHT + pointwise, 0 = everything.  LAY is the tile layout.
+//
+// Persistent CTAs: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x,
+// ...  Tiles are copied into a ring of p.nbuf shared-memory buffers
+// nbuf - 1 tiles ahead of the one being transformed and stored, so several
+// tiles of HBM reads are in flight per SM while the butterflies run: by TMA
+// boxes (one instruction per box, completion counted on an mbarrier) for
+// element-major tiles, by per-thread cp.async otherwise.  Element-major
+// results leave by TMA box stores.  Dynamic shared memory (launch_smem):
+// nbuf tile buffers, nbuf mbarriers, nbuf sets of VInfo records, per-vector
+// scalars.
+template <class E, int CLS, int LAY>
+__global__ void __launch_bounds__(FM_MAX_THREADS, 1)
     vprog_kernel(const __grid_constant__ Step p) {
-  extern __shared__ __align__(16) unsigned char fm_smem[];
-  E *sm = reinterpret_cast<E *>(fm_smem);
+  extern __shared__ __align__(128) unsigned char fm_smem[];
   const int tid = threadIdx.x, T = blockDim.x;
-  const int B = p.B, L = p.L, Lp = p.Lp;
-  const i64 gv0 = (i64)blockIdx.x * B;
+  const int B = p.B, Lp = p.Lp;
+  const int NB = p.nbuf;
+  const size_t tb = tile_bytes(B, Lp, sizeof(E));
+  unsigned long long *bars =
+      reinterpret_cast<unsigned long long *>(fm_smem + NB * tb);
+  VInfo *const vi0 = reinterpret_cast<VInfo *>(bars + NB);
+  i64 *sq = reinterpret_cast<i64 *>(vi0 + NB * B);
+  auto buf = [&](int k) { return reinterpret_cast<E *>(fm_smem + k * tb); };
+  auto vis = [&](int k) { return vi0 + k * B; };
   const i64 nvec = p.V * p.num_cols;
+  const i64 ntiles = (nvec + B - 1) / B;
+  const FDiv dV((unsigned)p.V), dci((unsigned)p.vin.Cc),
+      dco((unsigned)p.vout.Cc);
+  const bool tma_in = LAY == 1 && p.tma_in;
+  const bool tma_out = LAY == 1 && p.tma_out;
+  const bool async_in = tma_in || (p.src_type == Tr<E>::code && !p.map_in);
+  const bool fixup = p.conj_in || p.pre;
+  const i64 G = gridDim.x;
 
-  // ---- load: tile of B vectors, converted to E, zero padded to L
-  {
-    const bool strided = p.vin.Cc > 1;
-    const int total = B * L;
-    for (int f = tid; f < total; f += T) {
-      int b, j;
-      if (strided) {
-        j = f / B;
-        b = f - j * B;
-      } else {
-        b = f / L;
-        j = f - b * L;
-      }
-      const i64 gv = gv0 + b;
-      E val = zero<E>();
-      if (gv < nvec && j < p.in_len) {
-        const i64 m = gv / p.V, v = gv - m * p.V;
-        const i64 a = v / p.vin.Cc, c = v - a * p.vin.Cc;
-        const i64 r = (a * p.vin.n + j) * p.vin.Cc + c;
-        if (r < p.in_rows) {
-          const i64 srow = p.map_in ? p.map_in[r] : r;
-          if (srow >= 0) {
-            val = load_as<E>(p.src, p.src_type, m * p.ld_src + srow);
-            if (p.conj_in) val = conjv(val);
-            if (p.pre) val = mulv(val, ((const E *)p.pre)[r], false);
-          }
+  if (tma_in) {
+    if (tid == 0) {
+      for (int k = 0; k < NB; ++k) mbar_init(smem_addr(bars + k));
+      mbar_init_fence();
+    }
+    __syncthreads();
+  }
+
+  i64 tile = blockIdx.x;
+  // prologue: the first nbuf - 1 tiles
+  if (async_in) {
+    for (int k = 0; k < NB - 1; ++k) {
+      const i64 t = tile + k * G;
+      if (t < ntiles) {
+        setup_tile(p, vis(k), t, dV, dci, dco, nvec, tid, T);
+        if (tma_in) {
+          if (tid == 0) tma_issue_load<E>(p, buf(k), smem_addr(bars + k), t);
+        } else {
+          __syncthreads();
+          load_async<E, LAY>(p, buf(k), vis(k), tid, T);
         }
       }
-      sm[b * Lp + pidx<E>(j)] = val;
+      if (!tma_in) cp_async_commit();
     }
   }
-  __syncthreads();
-
-  // ---- program
-  for (int o = 0; o < p.nops; ++o) {
-    const Op &op = p.ops[o];
-    switch (op.kind) {
-      case OP_FFT:
-        if constexpr (Tr<E>::cplx && CLS != 3) run_fft<E, CLS>(op, sm, Lp, B, tid, T);
-        break;
-      case OP_FWHT:
-        if constexpr (CLS == 0 || CLS == 3) run_fwht<E>(op, sm, Lp, B, tid, T);
-        break;
-      case OP_GATHER:
-        if constexpr (CLS == 0) run_gather<E>(op, sm, Lp, B, tid, T);
-        break;
-      case OP_DENSE:
-        if constexpr (CLS == 0) run_dense<E>(op, sm, Lp, B, tid, T);
-        break;
-      case OP_ZPAD: run_zpad<E>(op, sm, Lp, B, tid, T); break;
-      default: run_elementwise<E>(op, sm, Lp, B, gv0, p.V, tid, T); break;
-    }
-  }
-
-  // ---- store
-  const bool acc = p.accumulate != 0;
-  if (p.out_mode == 1) {
-    // gather: out row i of column m takes vector element map_out[i]
-    for (int f = tid; f < B * p.n_out; f += T) {
-      const int b = f / p.n_out, i = f - b * p.n_out;
-      const i64 gv = gv0 + b;
-      if (gv >= nvec) continue;
-      const i64 m = gv / p.V;
-      const i64 j = p.map_out[i];
-      E val = j < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)j)];
-      if (j >= 0 && p.post) val = mulv(val, ((const E *)p.post)[j], false);
-      if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
-      if (p.conj_out) val = conjv(val);
-      store_as<E>(p.dst, p.dst_type, m * p.ld_dst + i, val, acc);
-    }
-    return;
-  }
-  const bool strided = p.vout.Cc > 1;
-  const int total = B * p.out_len;
-  for (int f = tid; f < total; f += T) {
-    int b, j;
-    if (strided) {
-      j = f / B;
-      b = f - j * B;
+  int cur = 0;
+  unsigned phase_bits = 0;  // bit k: parity of the next completion of bar k
+  bool failed = false;
+  while (tile < ntiles) {
+    E *sm = buf(cur);
+    VInfo *vi = vis(cur);
+    // per-thread loads refill buffers that a TMA store may still be
+    // reading: wait for those reads (a barrier follows before any refill)
+    if (tma_out && !tma_in && tid == 0) bulk_wait_read<0>();
+    if (async_in) {
+      if (!tma_in) {
+        const i64 ahead = tile + (NB - 1) * G;
+        int slot = cur + NB - 1;
+        if (slot >= NB) slot -= NB;
+        if (ahead < ntiles) {
+          setup_tile(p, vis(slot), ahead, dV, dci, dco, nvec, tid, T);
+          __syncthreads();
+          load_async<E, LAY>(p, buf(slot), vis(slot), tid, T);
+        }
+        cp_async_commit();
+        cp_async_wait_n(NB - 1);
+      } else {
+        const bool ok = mbar_wait(smem_addr(bars + cur),
+                                  (phase_bits >> cur) & 1u, FM_WAIT_LIMIT);
+        // block-wide vote so that every thread leaves the loop together
+        if (__syncthreads_or(!ok)) {
+          failed = true;
+          break;
+        }
+        phase_bits ^= 1u << cur;
+      }
+      __syncthreads();
+      if (fixup) {
+        load_fixup<E, LAY>(p, sm, vi, tid, T);
+        __syncthreads();
+      }
     } else {
-      b = f / p.out_len;
-      j = f - b * p.out_len;
+      setup_tile(p, vi, tile, dV, dci, dco, nvec, tid, T);
+      __syncthreads();
+      load_general<E, LAY>(p, sm, vi, tid, T);
+      __syncthreads();
     }
-    const i64 gv = gv0 + b;
-    if (gv >= nvec) continue;
-    const i64 m = gv / p.V, v = gv - m * p.V;
-    const i64 a = v / p.vout.Cc, c = v - a * p.vout.Cc;
-    const i64 r = (a * p.vout.n + j) * p.vout.Cc + c;
-    if (r >= p.out_rows) continue;
-    const i64 drow = p.out_mode == 2 ? p.map_out[r] : r;
-    if (drow < 0) continue;
-    E val = sm[b * Lp + pidx<E>(j)];
-    if (p.post) val = mulv(val, ((const E *)p.post)[r], false);
-    if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
-    if (p.conj_out) val = conjv(val);
-    store_as<E>(p.dst, p.dst_type, m * p.ld_dst + drow, val, acc);
+
+    run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T);
+
+    if (tma_out) {
+      store_fixup_em<E>(p, sm, vi, tid, T);
+      if (tid == 0) tma_issue_store<E>(p, sm, tile);
+    } else {
+      store_tile<E, LAY>(p, sm, vi, tid, T);
+    }
+    if (tma_in) {
+      // refill the buffer freed one iteration ago (tile - G) with the tile
+      // nbuf - 1 ahead, once its TMA store has finished reading it
+      const i64 ahead = tile + (NB - 1) * G;
+      int slot = cur + NB - 1;
+      if (slot >= NB) slot -= NB;
+      __syncthreads();
+      if (ahead < ntiles) {
+        setup_tile(p, vis(slot), ahead, dV, dci, dco, nvec, tid, T);
+        if (tid == 0) {
+          if (tma_out) bulk_wait_read<1>();
+          fence_async_smem();
+          tma_issue_load<E>(p, buf(slot), smem_addr(bars + slot), ahead);
+        }
+      }
+    }
+    __syncthreads();
+    if (++cur == NB) cur = 0;
+    tile += G;
   }
+  if (failed) {
+    if (tid == 0 && p.err) atomicExch(p.err, FM_ERR_TIMEOUT);
+    // let the loads still in flight (this tile and up to nbuf - 2 ahead)
+    // land before the CTA exits, again with bounded waits
+    for (int d = 0; d < NB - 1; ++d) {
+      int k = cur + d;
+      if (k >= NB) k -= NB;
+      if (tile + d * G < ntiles)
+        mbar_wait(smem_addr(bars + k), (phase_bits >> k) & 1u, FM_WAIT_LIMIT);
+    }
+  }
+  if (tma_out && tid == 0) bulk_wait_all();
+  if (!tma_in) cp_async_wait<0>();
 }
 
 }  // namespace fmk

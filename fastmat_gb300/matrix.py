@@ -303,6 +303,7 @@ class Matrix:
                      n_req, yt.data_ptr(), _native.DTYPE_CODE[out_dt], n_out,
                      M, stream)
         y = yt.cpu().numpy().T
+        plan.check()
         return y.reshape(n_out) if flat else y
 
     def _transform_device(self, x, direction):

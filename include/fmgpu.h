@@ -179,6 +179,13 @@ int fm_execute_host(fm_plan *plan, int32_t direction,
                     void *y, int32_t y_type, int64_t ld_y,
                     int64_t num_cols);
 
+/* Report (and clear) a failure that kernels of this plan recorded on the
+ * device since the last check: FM_ERR_TIMEOUT if a bounded wait for a tile
+ * copy gave up.  Synchronises with the device.  fm_execute_host checks on
+ * every call; callers of the asynchronous entry points check after they
+ * synchronise.  The reference has no device and no counterpart. */
+int fm_plan_check(fm_plan *plan);
+
 int fm_plan_destroy(fm_plan *plan);
 
 /* Plan introspection for tests and benchmarks. */
