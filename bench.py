@@ -229,6 +229,9 @@ def run_gpu(args):
     clocks = ClockSampler('GPU-%s' % uuid if uuid is not None else dev)
     ref_y = None
     for name, op, dt in (('fp64', op64, dt64), ('fp32', op32, dt32)):
+        # plan creation includes the autotuner's choice of tile shapes
+        if not args.no_autotune:
+            op.autotune(M, out_dtype=op._output_dtype(np.dtype(dt)))
         x = make_input(n_in, M, dt, 1000 + rank)
         xt = torch.from_numpy(x.T).cuda().t()  # column-major device tensor
         if name == 'fp64':
@@ -453,6 +456,7 @@ def main():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--workload', default='kron', choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-autotune', action='store_true')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -31,6 +31,10 @@ DTYPE_CODE = {
 }
 CODE_DTYPE = {v: k for k, v in DTYPE_CODE.items()}
 
+# compute types: float64 / complex128 in double-float arithmetic
+FM_F64_DF = 16
+FM_C128_DF = 17
+
 (NODE_FOURIER, NODE_CIRCULANT, NODE_TOEPLITZ, NODE_HADAMARD, NODE_DIAG,
  NODE_PARTIAL, NODE_PERMUTATION, NODE_PRODUCT, NODE_SUM, NODE_KRON,
  NODE_HERMITIAN, NODE_CONJUGATE, NODE_EYE, NODE_DENSE) = range(1, 15)
@@ -67,6 +71,7 @@ class FmPlanInfo(ctypes.Structure):
 #: every entry point include/fmgpu.h declares
 EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
            'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
+           'fm_plan_set_tile', 'fm_plan_get_tile', 'fm_plan_autotune',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
            'fm_last_error', 'fm_version')
 
@@ -75,7 +80,9 @@ _lock = threading.Lock()
 
 
 def library_path():
-    return _build.LIB
+    """The engine library: FASTMAT_GB300_LIB if set (a custom build),
+    else the in-tree libfmgpu.so."""
+    return os.environ.get('FASTMAT_GB300_LIB') or _build.LIB
 
 
 def load(build_if_missing=True):
@@ -108,6 +115,14 @@ def load(build_if_missing=True):
         lib.fm_execute_static.restype = ctypes.c_int
         lib.fm_execute_host.argtypes = [P, I32, P, I32, I64, P, I32, I64, I64]
         lib.fm_execute_host.restype = ctypes.c_int
+        lib.fm_plan_set_tile.argtypes = [P, I32, I32, I32, I32]
+        lib.fm_plan_set_tile.restype = ctypes.c_int
+        lib.fm_plan_get_tile.argtypes = [P, I32, I32, ctypes.POINTER(I32),
+                                         ctypes.POINTER(I32),
+                                         ctypes.POINTER(I32)]
+        lib.fm_plan_get_tile.restype = ctypes.c_int
+        lib.fm_plan_autotune.argtypes = [P, I32, I64, P]
+        lib.fm_plan_autotune.restype = ctypes.c_int
         lib.fm_plan_check.argtypes = [P]
         lib.fm_plan_check.restype = ctypes.c_int
         lib.fm_plan_destroy.argtypes = [P]
@@ -180,6 +195,31 @@ class Plan:
             self.handle, direction, x.ctypes.data, DTYPE_CODE[x.dtype],
             x.shape[0], y.ctypes.data, DTYPE_CODE[y.dtype], y.shape[0],
             x.shape[1]))
+
+    def tiles(self, direction):
+        """[(vectors_per_tile, nbuf, layout)] of every launch."""
+        out = []
+        for k in range(self.num_launches(direction)):
+            b, n, lay = (ctypes.c_int32(), ctypes.c_int32(),
+                         ctypes.c_int32())
+            check(self._lib.fm_plan_get_tile(self.handle, direction, k,
+                                             ctypes.byref(b), ctypes.byref(n),
+                                             ctypes.byref(lay)))
+            out.append((b.value, n.value, lay.value))
+        return out
+
+    def set_tiles(self, direction, tiles):
+        for k, (b, n, _lay) in enumerate(tiles):
+            check(self._lib.fm_plan_set_tile(self.handle, direction, k, b, n))
+
+    def num_launches(self, direction):
+        inf = self.info()
+        return (inf.num_launches_fwd if direction == FORWARD
+                else inf.num_launches_bwd)
+
+    def autotune(self, direction, num_cols, stream=None):
+        check(self._lib.fm_plan_autotune(self.handle, direction, num_cols,
+                                         stream))
 
     def check(self):
         """Raise if a kernel of this plan reported a failure (syncs)."""

@@ -17,6 +17,10 @@ cudaError_t launch_c64(const Step &st, int cls, int lay, int threads,
                        size_t smem, i64 grid, cudaStream_t s);
 cudaError_t launch_c128(const Step &st, int cls, int lay, int threads,
                        size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_df(const Step &st, int cls, int lay, int threads,
+                      size_t smem, i64 grid, cudaStream_t s);
+cudaError_t launch_dfc(const Step &st, int cls, int lay, int threads,
+                       size_t smem, i64 grid, cudaStream_t s);
 cudaError_t launch_i64(const Step &st, int cls, int lay, int threads,
                        size_t smem, i64 grid, cudaStream_t s);
 

@@ -54,6 +54,8 @@ struct Error {
 
 int esize(int t) {
   switch (t) {
+    case FM_F64_DF: return 8;
+    case FM_C128_DF: return 16;
     case FM_I8: return 1;
     case FM_I16: return 2;
     case FM_I32: return 4;
@@ -65,7 +67,13 @@ int esize(int t) {
     default: return 0;
   }
 }
-bool is_cplx(int t) { return t == FM_C64 || t == FM_C128; }
+bool is_cplx(int t) {
+  return t == FM_C64 || t == FM_C128 || t == FM_C128_DF;
+}
+// element type of the buffers a plan of compute type t reads and writes
+int io_of(int t) {
+  return t == FM_F64_DF ? FM_F64 : t == FM_C128_DF ? FM_C128 : t;
+}
 bool valid_type(int t) { return t >= FM_I8 && t <= FM_C128; }
 
 cd host_get(const void *p, int t, i64 i) {
@@ -121,6 +129,12 @@ template <> __device__ float2 mk<float2>(double re, double im) {
 }
 template <> __device__ double2 mk<double2>(double re, double im) {
   return make_double2(re, im);
+}
+template <> __device__ fmk::df mk<fmk::df>(double re, double) {
+  return fmk::d2df(re);
+}
+template <> __device__ fmk::dfc mk<fmk::dfc>(double re, double im) {
+  return fmk::dfc{fmk::d2df(re), fmk::d2df(im)};
 }
 
 // tw[t] = exp(-2 pi i t / N); the phase t/N is exact in integers and the
@@ -184,6 +198,7 @@ struct LStep {
   int cls, threads;
   size_t smem;
   int lay = 0;                     // tile layout (1: element-major)
+  int ept = 8;                     // elements per thread of its class
   int tma_in_ok = 0, tma_out_ok = 0;  // views allow TMA boxes
   // last encoded tensor maps and the (address, ld, columns) they describe
   const void *tm_in_key = nullptr, *tm_out_key = nullptr;
@@ -194,7 +209,8 @@ struct LStep {
 }  // namespace
 
 struct fm_plan {
-  int ctype = FM_C128;
+  int ctype = FM_C128;  // compute type (FM_* or FM_*_DF)
+  int io_type = FM_C128;  // element type of scratch buffers
   int esz = 16;
   int device = 0;
   i64 rows = 0, cols = 0;
@@ -273,6 +289,109 @@ fmk::Op mkop(int kind, int len) {
   return o;
 }
 
+// Tile configuration of one launch: layout, vectors per tile (B), threads,
+// copy-ring depth and shared memory.  want_B / want_nbuf = 0 picks the
+// heuristic choice; explicit values (the autotuner's candidates) are
+// accepted when feasible.  Returns false if the request cannot be met.
+bool configure(int esz, LStep &ls, int want_B, int want_nbuf) {
+  fmk::Step &st = ls.st;
+  const int L = std::max(st.L, 1);
+  const int ept = ls.ept;
+  auto threads_for = [&](int b) {
+    i64 t = ((i64)b * L + ept - 1) / ept;
+    t = (t + 31) / 32 * 32;
+    return (int)std::max<i64>(t, 32);
+  };
+  auto pick_nbuf = [&](int B, int Lp) {
+    if (want_nbuf) return want_nbuf;
+    int nb = 4;
+    while (nb > 2 && fmk::launch_smem(B, Lp, esz, nb) > (size_t)150 * 1024)
+      --nb;
+    return nb;
+  };
+  const bool pow2 = want_B == 0 || (want_B & (want_B - 1)) == 0;
+  if (!pow2 || want_nbuf < 0 || want_nbuf == 1 || want_nbuf > 4) return false;
+
+  // element-major tiles: strided input and output views whose inner extent
+  // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
+  // budget allows, never below 16 B), moved by TMA boxes
+  if ((ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 && st.vout.Cc > 1) {
+    int B = want_B ? want_B : 128 / esz;
+    if (!want_B) {
+      while (B > 1 && (st.vin.Cc % B || st.vout.Cc % B)) B /= 2;
+      while (B * esz > 16 && threads_for(B) > FM_MAX_THREADS) B /= 2;
+    }
+    if (B * esz >= 16 && threads_for(B) <= FM_MAX_THREADS &&
+        st.V % B == 0 && st.vin.Cc % B == 0 && st.vout.Cc % B == 0) {
+      const int nbuf = pick_nbuf(B, L);
+      const size_t smem = fmk::launch_smem(B, L, esz, nbuf);
+      if (smem <= (size_t)fmk::kMaxSmem) {
+        ls.lay = 1;
+        st.B = B;
+        st.Lp = L;
+        st.nbuf = nbuf;
+        st.box_rows = std::min(L, 256);
+        st.elem_k = esz == 16 ? 2 : 1;
+        const bool rows_ok = L % st.box_rows == 0;
+        ls.tma_in_ok = rows_ok && st.in_len == st.vin.n && !st.map_in &&
+                       st.in_rows == st.vin.A * st.vin.n * st.vin.Cc;
+        ls.tma_out_ok = rows_ok && st.out_len == st.vout.n &&
+                        st.out_mode == 0 && !st.accumulate &&
+                        st.out_rows == st.vout.A * st.vout.n * st.vout.Cc;
+        ls.threads = threads_for(B);
+        ls.smem = smem;
+        return true;
+      }
+    }
+    if (want_B) return false;
+  }
+
+  // vector-major tiles, padded: one 16-byte granule per 128 bytes (pidx),
+  // rounded to whole granules, with an odd granule count so that
+  // consecutive vectors start on different banks
+  const int shift = esz >= 16 ? 3 : (esz == 8 ? 4 : 5);
+  const int gran = 16 / esz;
+  int Lp = (L - 1) + gran * ((L - 1) >> shift) + 1;
+  Lp = (Lp + gran - 1) / gran * gran;
+  if (((Lp / gran) & 1) == 0) Lp += gran;
+  const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
+  auto smem_for = [&](int b, int nb) {
+    return fmk::launch_smem(b, Lp, esz, nb);
+  };
+  int B;
+  if (want_B) {
+    B = want_B;
+  } else {
+    B = strided ? std::max(1, 128 / esz) : 1;
+    const size_t budget = 110 * 1024;
+    while (B > 1 && (threads_for(B) > FM_MAX_THREADS ||
+                     smem_for(B, 2) > (size_t)fmk::kMaxSmem))
+      B /= 2;
+    while (threads_for(B) < 128 && threads_for(2 * B) <= FM_MAX_THREADS &&
+           smem_for(2 * B, 2) <= budget && (i64)B < st.V * 64 && B < 1024)
+      B *= 2;
+  }
+  if (threads_for(B) > FM_MAX_THREADS) return false;
+  const int nbuf = pick_nbuf(B, Lp);
+  const size_t smem = smem_for(B, nbuf);
+  if (smem > (size_t)fmk::kMaxSmem) return false;
+  ls.lay = 0;
+  st.B = B;
+  st.Lp = Lp;
+  st.nbuf = nbuf;
+  ls.threads = threads_for(B);
+  ls.smem = smem;
+  // contiguous vectors move by 1-D bulk copies of their 128-byte chunks
+  ls.tma_in_ok = st.vin.Cc == 1 && st.in_len == L && st.in_len == st.vin.n &&
+                 !st.map_in && st.in_rows == st.vin.A * st.vin.n &&
+                 ((i64)st.in_len * esz) % 16 == 0;
+  ls.tma_out_ok = st.vout.Cc == 1 && st.out_len == st.vout.n &&
+                  st.out_mode == 0 && !st.accumulate &&
+                  st.out_rows == st.vout.A * st.vout.n &&
+                  ((i64)st.out_len * esz) % 16 == 0;
+  return true;
+}
+
 class Planner {
  public:
   Planner(fm_plan *P, const std::vector<NodeRec> &nodes)
@@ -318,6 +437,8 @@ class Planner {
     void *p = dalloc((size_t)N * P_->esz);
     if (P_->ctype == FM_C64)
       k_twiddle<float2><<<grid_for(N), 256>>>((float2 *)p, N);
+    else if (P_->ctype == FM_C128_DF)
+      k_twiddle<fmk::dfc><<<grid_for(N), 256>>>((fmk::dfc *)p, N);
     else
       k_twiddle<double2><<<grid_for(N), 256>>>((double2 *)p, N);
     CUDA_TRY(cudaGetLastError());
@@ -330,7 +451,19 @@ class Planner {
     const size_t n = v.size();
     std::vector<unsigned char> buf(n * P_->esz);
     for (size_t i = 0; i < n; ++i) {
+      auto hi = [](double d) { return (float)d; };
+      auto lo = [](double d) { return (float)(d - (double)(float)d); };
       switch (P_->ctype) {
+        case FM_F64_DF:
+          ((float *)buf.data())[2 * i] = hi(v[i].real());
+          ((float *)buf.data())[2 * i + 1] = lo(v[i].real());
+          break;
+        case FM_C128_DF:
+          ((float *)buf.data())[4 * i] = hi(v[i].real());
+          ((float *)buf.data())[4 * i + 1] = lo(v[i].real());
+          ((float *)buf.data())[4 * i + 2] = hi(v[i].imag());
+          ((float *)buf.data())[4 * i + 3] = lo(v[i].imag());
+          break;
         case FM_F32: ((float *)buf.data())[i] = (float)v[i].real(); break;
         case FM_F64: ((double *)buf.data())[i] = v[i].real(); break;
         case FM_I64:
@@ -393,6 +526,7 @@ class Planner {
     sub[0].d = nd;
     fm_plan Q;
     Q.ctype = FM_C128;
+    Q.io_type = FM_C128;
     Q.esz = 16;
     Q.device = P_->device;
     Q.rows = Q.cols = L;
@@ -425,6 +559,9 @@ class Planner {
     if (P_->ctype == FM_C64)
       k_convert<float2><<<grid_for(n), 256>>>((float2 *)p, src, n, scale, L1,
                                                L2);
+    else if (P_->ctype == FM_C128_DF)
+      k_convert<fmk::dfc><<<grid_for(n), 256>>>((fmk::dfc *)p, src, n, scale,
+                                                 L1, L2);
     else
       k_convert<double2><<<grid_for(n), 256>>>((double2 *)p, src, n, scale,
                                                 L1, L2);
@@ -575,7 +712,8 @@ class Planner {
         r.push_back(p);
         n /= p;
       }
-    const int big = 16;
+    // largest radix: 16, except 8 for double-float (register budget)
+    const int big = P_->ctype == FM_C128_DF ? 8 : 16;
     while (n % big == 0) {
       r.push_back(big);
       n /= big;
@@ -847,7 +985,15 @@ class Planner {
           c.push_back(prog({fwht_op(N)}, N, N, N));
           return c;
         }
-        const int p1 = (int)(d.n / 2), p2 = (int)(d.n - p1);
+        // widest contiguous pass that fits one tile, the rest strided (so
+        // the strided pass keeps wide TMA rows)
+        int p2 = 0;
+        while ((2LL << p2) <= lmax_ && p2 + 1 < d.n) ++p2;
+        int p1 = (int)(d.n - p2);
+        if ((1LL << p1) > lmax_) {
+          p1 = (int)(d.n / 2);
+          p2 = (int)(d.n - p1);
+        }
         const i64 N1 = 1LL << p1, N2 = 1LL << p2;
         Unit u;
         u.kind = Unit::STEPS;
@@ -1108,82 +1254,10 @@ class Planner {
     st.nops = (int)ops.size();
     for (size_t i = 0; i < ops.size(); ++i) st.ops[i] = ops[i];
     ls.cls = kernel_class(ops);
-    bool odd = ls.cls == 2 || ls.cls == 0;
-    const int ept = odd ? ept_ / 2 : ept_;
-    const int L = std::max(st.L, 1);
-    const int esz = P_->esz;
-    auto threads_for = [&](int b) {
-      i64 t = ((i64)b * L + ept - 1) / ept;
-      t = (t + 31) / 32 * 32;
-      return (int)std::max<i64>(t, 32);
-    };
-    const i64 nvec = st.V;  // per column; tiles may span columns
-
-    // element-major tiles: strided input and output views whose inner
-    // extent holds whole tiles (B | Cc); rows of B * esz bytes (128 B when
-    // the thread budget allows, never below 16 B), moved by TMA boxes
-    ls.lay = 0;
-    ls.tma_in_ok = ls.tma_out_ok = 0;
-    if ((ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 && st.vout.Cc > 1) {
-      int B = 128 / esz;
-      while (B > 1 && (st.vin.Cc % B || st.vout.Cc % B)) B /= 2;
-      while (B * esz > 16 && threads_for(B) > FM_MAX_THREADS) B /= 2;
-      if (B * esz >= 16 && threads_for(B) <= FM_MAX_THREADS &&
-          st.V % B == 0) {
-        ls.lay = 1;
-        st.B = B;
-        st.Lp = L;
-        st.box_rows = std::min(L, 256);
-        st.elem_k = esz == 16 ? 2 : 1;
-        const bool rows_ok = L % st.box_rows == 0;
-        ls.tma_in_ok = rows_ok && st.in_len == st.vin.n && !st.map_in &&
-                       st.in_rows == st.vin.A * st.vin.n * st.vin.Cc;
-        ls.tma_out_ok = rows_ok && st.out_len == st.vout.n &&
-                        st.out_mode == 0 && !st.accumulate &&
-                        st.out_rows == st.vout.A * st.vout.n * st.vout.Cc;
-        ls.threads = threads_for(B);
-        int nbuf = 4;
-        while (nbuf > 2 &&
-               fmk::launch_smem(B, L, esz, nbuf) > (size_t)150 * 1024)
-          --nbuf;
-        st.nbuf = nbuf;
-        ls.smem = fmk::launch_smem(B, L, esz, nbuf);
-        if (ls.smem <= (size_t)fmk::kMaxSmem) return;
-        ls.lay = 0;  // does not fit: fall back to vector-major tiles
-        ls.tma_in_ok = ls.tma_out_ok = 0;
-      }
-    }
-
-    const int shift = esz >= 16 ? 3 : (esz == 8 ? 4 : 5);
-    int Lp = (L - 1) + ((L - 1) >> shift) + 1;
-    if ((Lp & 1) == 0) ++Lp;
-    st.Lp = Lp;
-    const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
-    int B = 1;
-    if (strided) B = std::max(1, 128 / esz);
-    const size_t budget = 110 * 1024;
-    // dynamic shared memory of a tile of b vectors: the vectors, then one
-    // addressing record and one scalar per vector
-    auto smem_for = [&](int b) { return fmk::launch_smem(b, Lp, esz, 2); };
-    while (B > 1 && (threads_for(B) > FM_MAX_THREADS ||
-                     smem_for(B) > (size_t)fmk::kMaxSmem))
-      B /= 2;
-    while (threads_for(B) < 128 && threads_for(2 * B) <= FM_MAX_THREADS &&
-           smem_for(2 * B) <= budget && (i64)B < nvec * 64 && B < 1024)
-      B *= 2;
-    if (threads_for(B) > FM_MAX_THREADS)
+    const bool odd = ls.cls == 2 || ls.cls == 0;
+    ls.ept = odd ? ept_ / 2 : ept_;
+    if (!configure(P_->esz, ls, 0, 0))
       fail(FM_ERR_UNSUPPORTED, "working length too large for one tile");
-    st.B = B;
-    ls.threads = threads_for(B);
-    // deepest cp.async ring (up to 4 tiles) within ~150 KB per CTA
-    int nbuf = 4;
-    while (nbuf > 2 &&
-           fmk::launch_smem(B, Lp, esz, nbuf) > (size_t)150 * 1024)
-      --nbuf;
-    st.nbuf = nbuf;
-    ls.smem = fmk::launch_smem(B, Lp, esz, nbuf);
-    if (ls.smem > (size_t)fmk::kMaxSmem)
-      fail(FM_ERR_UNSUPPORTED, "tile exceeds shared memory");
   }
 
   fmk::Step base_step() {
@@ -1355,7 +1429,10 @@ class Planner {
             Unit cp = prog({}, u.n_out, u.n_out, u.n_out);
             std::vector<LStep> acc;
             emit_prog(cp, tmp, dst, acc);
-            for (LStep &a : acc) a.st.accumulate = 1;
+            for (LStep &a : acc) {
+              a.st.accumulate = 1;
+              a.tma_out_ok = 0;  // accumulation reads the destination
+            }
             out.insert(out.end(), acc.begin(), acc.end());
           }
           break;
@@ -1428,8 +1505,20 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
   st.err = P->err;
   st.tma_in = st.tma_out = 0;
+  if (ls.lay == 0) {
+    const int esz = P->esz;
+    auto aligned = [&](const void *ptr, i64 ld, i64 n) {
+      return ((uintptr_t)ptr & 15) == 0 && (ld * esz) % 16 == 0 &&
+             (n * esz) % 16 == 0;
+    };
+    st.tma_in = ls.tma_in_ok && st.src_type == P->io_type &&
+                aligned(st.src, st.ld_src, st.vin.n);
+    st.tma_out = ls.tma_out_ok && !st.accumulate &&
+                 st.dst_type == P->io_type &&
+                 aligned(st.dst, st.ld_dst, st.vout.n);
+  }
   if (ls.lay == 1) {
-    if (ls.tma_in_ok && st.src_type == P->ctype) {
+    if (ls.tma_in_ok && st.src_type == P->io_type) {
       if (ls.tm_in_key != st.src || ls.tm_in_ld != st.ld_src ||
           ls.tm_in_m != st.num_cols) {
         ls.tm_in_key = nullptr;
@@ -1445,7 +1534,7 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
         st.tma_in = 1;
       }
     }
-    if (ls.tma_out_ok && st.dst_type == P->ctype) {
+    if (ls.tma_out_ok && !st.accumulate && st.dst_type == P->io_type) {
       if (ls.tm_out_key != st.dst || ls.tm_out_ld != st.ld_dst ||
           ls.tm_out_m != st.num_cols) {
         ls.tm_out_key = nullptr;
@@ -1471,6 +1560,8 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
     case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_F64_DF: e = fmk::launch_df(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_C128_DF: e = fmk::launch_dfc(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     default: e = fmk::launch_c128(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
   }
   CUDA_TRY(e);
@@ -1515,7 +1606,7 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
         ld = ld_y;
       } else {
         ptr = (char *)P->scratch + offs[id - 2];
-        type = P->ctype;
+        type = P->io_type;
         ld = P->scratch_rows[id - 2];
       }
     };
@@ -1591,7 +1682,7 @@ int run_plan_static(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
         ld = ld_y;
       } else {
         ptr = base + offs[id - 2];
-        type = P->ctype;
+        type = P->io_type;
         ld = P->scratch_rows[id - 2];
       }
     };
@@ -1655,7 +1746,8 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
       fail(FM_ERR_VALUE, "invalid node array");
     if (compute_type != FM_F32 && compute_type != FM_F64 &&
         compute_type != FM_C64 && compute_type != FM_C128 &&
-        compute_type != FM_I64)
+        compute_type != FM_I64 && compute_type != FM_F64_DF &&
+        compute_type != FM_C128_DF)
       fail(FM_ERR_TYPE, "unsupported compute type");
     std::vector<NodeRec> recs((size_t)num_nodes);
     for (int i = 0; i < num_nodes; ++i) {
@@ -1675,6 +1767,7 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
     }
     std::unique_ptr<fm_plan> P(new fm_plan);
     P->ctype = compute_type;
+    P->io_type = io_of(compute_type);
     P->esz = esize(compute_type);
     CUDA_TRY(cudaGetDevice(&P->device));
     P->rows = nodes[root].rows;
@@ -1799,6 +1892,124 @@ int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
     CUDA_TRY(cudaMemcpyAsync(y, plan->dy, by, cudaMemcpyDeviceToHost,
                              plan->hstream));
     CUDA_TRY(cudaStreamSynchronize(plan->hstream));
+    return fm_plan_check(plan);
+  });
+}
+
+int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,
+                     int32_t vectors_per_tile, int32_t nbuf) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    std::vector<LStep> &steps = plan->steps[direction];
+    if (launch < 0 || launch >= (int)steps.size())
+      fail(FM_ERR_VALUE, "launch index out of range");
+    LStep &ls = steps[launch];
+    const LStep keep = ls;
+    if (!configure(plan->esz, ls, vectors_per_tile, nbuf)) {
+      ls = keep;
+      fail(FM_ERR_VALUE, "tile configuration not feasible for this launch");
+    }
+    return FM_OK;
+  });
+}
+
+int fm_plan_get_tile(const fm_plan *plan, int32_t direction, int32_t launch,
+                     int32_t *vectors_per_tile, int32_t *nbuf,
+                     int32_t *layout) {
+  return guarded([&]() {
+    if (!plan || !vectors_per_tile || !nbuf || !layout)
+      fail(FM_ERR_VALUE, "NULL argument");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    const std::vector<LStep> &steps = plan->steps[direction];
+    if (launch < 0 || launch >= (int)steps.size())
+      fail(FM_ERR_VALUE, "launch index out of range");
+    *vectors_per_tile = steps[launch].st.B;
+    *nbuf = steps[launch].st.nbuf;
+    *layout = steps[launch].lay;
+    return FM_OK;
+  });
+}
+
+int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
+                     void *stream) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    if (num_cols <= 0) fail(FM_ERR_VALUE, "num_cols must be positive");
+    const cudaStream_t s = (cudaStream_t)stream;
+    const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
+    const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
+    auto rows_of = [&](int id) {
+      return id == 0 ? n_in : id == 1 ? n_out : plan->scratch_rows[id - 2];
+    };
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    void *tsrc = nullptr, *tdst = nullptr;
+    try {
+      for (LStep &ls : plan->steps[direction]) {
+        const i64 rs = rows_of(ls.src), rd = rows_of(ls.dst);
+        // a sample of the columns, at most ~512 MiB per operand
+        const i64 cap = std::max<i64>(
+            1, (512ll << 20) / (std::max(rs, rd) * plan->esz));
+        const i64 M = std::min<i64>(num_cols, cap);
+        CUDA_TRY(cudaMalloc(&tsrc, (size_t)(rs * M * plan->esz)));
+        CUDA_TRY(cudaMalloc(&tdst, (size_t)(rd * M * plan->esz)));
+        // normal numbers (0x3F bytes) so that no fast path for zeros runs
+        CUDA_TRY(cudaMemsetAsync(tsrc, 0x3F, (size_t)(rs * M * plan->esz), s));
+        CUDA_TRY(cudaMemsetAsync(tdst, 0x3F, (size_t)(rd * M * plan->esz), s));
+        const LStep base = ls;
+        float best = 1e30f;
+        int bestB = base.st.B, bestN = base.st.nbuf;
+        for (int B = 1; B <= 1024; B *= 2) {
+          for (int nb = 2; nb <= 4; ++nb) {
+            ls = base;
+            if (!configure(plan->esz, ls, B, nb)) continue;
+            fmk::Step st = ls.st;
+            st.src = tsrc;
+            st.dst = tdst;
+            st.src_type = st.dst_type = plan->io_type;
+            st.ld_src = rs;
+            st.ld_dst = rd;
+            st.num_cols = M;
+            launch_step(plan, ls, st, s);  // warm-up
+            float t = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+              CUDA_TRY(cudaEventRecord(e0, s));
+              launch_step(plan, ls, st, s);
+              CUDA_TRY(cudaEventRecord(e1, s));
+              CUDA_TRY(cudaEventSynchronize(e1));
+              float ms = 0.f;
+              CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+              t = std::min(t, ms);
+            }
+            if (t < best) {
+              best = t;
+              bestB = B;
+              bestN = nb;
+            }
+          }
+        }
+        ls = base;
+        if (!configure(plan->esz, ls, bestB, bestN)) ls = base;
+        ls.tm_in_key = ls.tm_out_key = nullptr;  // descriptors of the temps
+        cudaFree(tsrc);
+        cudaFree(tdst);
+        tsrc = tdst = nullptr;
+      }
+    } catch (...) {
+      if (tsrc) cudaFree(tsrc);
+      if (tdst) cudaFree(tdst);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     return fm_plan_check(plan);
   });
 }

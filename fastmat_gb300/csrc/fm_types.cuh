@@ -17,6 +17,131 @@ namespace fmk {
 
 typedef long long i64;
 
+// ---------------------------------------------------------------- double-float
+// A double-float number is an unevaluated sum h + l of two floats with
+// |l| <= ulp(h) / 2, carrying a 48-bit significand (relative precision about
+// 2^-48) on the FP32 pipes.  Sums use Knuth's TwoSum, products Dekker's
+// TwoProduct through the fused multiply-add (both error-free
+// transformations), each followed by a renormalisation (Fast2Sum).  The
+// sum is the "sloppy" variant: its error is bounded by 2^-46 (|a| + |b|),
+// the norm-wise bound an FFT error analysis needs.
+struct df {
+  float h, l;
+  df() = default;
+  __host__ __device__ constexpr df(float h_, float l_) : h(h_), l(l_) {}
+  // compile-time constants: split a double literal into two floats
+  __host__ __device__ constexpr df(double d)
+      : h((float)d), l((float)(d - (double)(float)d)) {}
+  __host__ __device__ constexpr df(int i) : h((float)i), l(0.f) {}
+};
+struct dfc {
+  df x, y;  // real, imaginary
+};
+
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return df(s, b - (s - a));
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float e = (a.h - (s - bb)) + (b.h - bb) + (a.l + b.l);
+  return fast_two_sum(s, e);
+}
+__device__ __forceinline__ df operator-(df a) { return df(-a.h, -a.l); }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+// sign * x for sign = +1 / -1
+__device__ __forceinline__ df operator*(int s, df a) { return s < 0 ? -a : a; }
+__device__ __forceinline__ float smul(int s, float a) { return s < 0 ? -a : a; }
+__device__ __forceinline__ double smul(int s, double a) {
+  return s < 0 ? -a : a;
+}
+__device__ __forceinline__ df smul(int s, df a) { return s < 0 ? -a : a; }
+
+__device__ __forceinline__ dfc operator+(dfc a, dfc b) {
+  return dfc{a.x + b.x, a.y + b.y};
+}
+__device__ __forceinline__ dfc operator-(dfc a, dfc b) {
+  return dfc{a.x - b.x, a.y - b.y};
+}
+__device__ __forceinline__ dfc cmul(dfc a, dfc b) {
+  return dfc{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__device__ __forceinline__ dfc cmulc(dfc a, dfc b) {
+  return dfc{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+
+// double -> double-float with integer operations only (the FP64 pipe of
+// this GPU is slow): h is d rounded to 24 bits, l the float nearest to the
+// exact remainder d - h.  Zeros, subnormals and values outside the float
+// exponent range map to (0, 0) / (+-inf, 0).
+__device__ __forceinline__ df d2df(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sgn = (unsigned)(b >> 63) << 31;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0) return df(0.f, 0.f);
+  int e = ex - 1023;
+  if (ex == 0x7FF || e > 127)
+    return df(__int_as_float((int)(sgn | 0x7F800000u)), 0.f);
+  if (e < -126) return df(0.f, 0.f);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned long long mh = m >> 29;  // 24 bits
+  const unsigned long long rem = m & 0x1FFFFFFFull;
+  const unsigned long long half = 1ull << 28;
+  if (rem > half || (rem == half && (mh & 1))) ++mh;
+  // remainder relative to the rounded head: m - mh * 2^29 (|.| <= 2^28)
+  const long long r = (long long)m - (long long)(mh << 29);
+  if (mh == (1ull << 24)) {  // rounding carried into the next binade
+    mh >>= 1;
+    ++e;
+    if (e > 127) return df(__int_as_float((int)(sgn | 0x7F800000u)), 0.f);
+  }
+  const float h = __int_as_float(
+      (int)(sgn | ((unsigned)(e + 127) << 23) | (unsigned)(mh & 0x7FFFFF)));
+  // l = r * 2^(e0 - 52) with e0 the exponent before any carry
+  const int el = ex - 1023 - 52;
+  float l = (float)(int)r;  // |r| <= 2^28: rounds to 24 bits
+  if (el >= -126) {
+    l *= __int_as_float((el + 127) << 23);
+  } else if (el >= -126 - 23) {
+    l *= __int_as_float((el + 127 + 24) << 23);
+    l *= __int_as_float((127 - 24) << 23);
+  } else {
+    l = 0.f;
+  }
+  if (sgn) l = -l;
+  return df(h, l);
+}
+
+// double-float -> double: widen both floats exactly (bit manipulation) and
+// add once in double precision
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = (unsigned)__float_as_int(f);
+  const unsigned long long sg = (unsigned long long)(u >> 31) << 63;
+  const unsigned ex = (u >> 23) & 0xFF;
+  const unsigned long long mt = u & 0x7FFFFF;
+  if (ex == 0) {
+    if (mt == 0) return __longlong_as_double((long long)sg);
+    return (double)f;  // subnormal float: rare, let the hardware widen it
+  }
+  if (ex == 0xFF)
+    return __longlong_as_double(
+        (long long)(sg | 0x7FF0000000000000ull | (mt << 29)));
+  return __longlong_as_double(
+      (long long)(sg | ((unsigned long long)(ex - 127 + 1023) << 52) |
+                  (mt << 29)));
+}
+__device__ __forceinline__ double df2d(df a) {
+  return f2d_exact(a.h) + f2d_exact(a.l);
+}
+
 // ---------------------------------------------------------------- traits
 template <class E> struct Tr;
 template <> struct Tr<float> {
@@ -44,18 +169,32 @@ template <> struct Tr<i64> {
   static constexpr int code = FM_I64;
   typedef i64 R;
 };
+// double-float types hold (complex) float64 data: their buffers in global
+// memory are float64 / complex128, converted on load and store (emu)
+template <> struct Tr<df> {
+  static constexpr bool cplx = false;
+  static constexpr int code = FM_F64;
+  typedef df R;
+};
+template <> struct Tr<dfc> {
+  static constexpr bool cplx = true;
+  static constexpr int code = FM_C128;
+  typedef df R;
+};
+template <class E> struct Emu { static constexpr bool v = false; };
+template <> struct Emu<df> { static constexpr bool v = true; };
+template <> struct Emu<dfc> { static constexpr bool v = true; };
 
-// shared-memory padding: one spare element per 128 bytes keeps strided
-// butterfly accesses spread over all banks.
-template <class E> struct PadShift;
-template <> struct PadShift<float> { static constexpr int v = 5; };
-template <> struct PadShift<double> { static constexpr int v = 4; };
-template <> struct PadShift<i64> { static constexpr int v = 4; };
-template <> struct PadShift<float2> { static constexpr int v = 4; };
-template <> struct PadShift<double2> { static constexpr int v = 3; };
+// shared-memory padding: one spare 16-byte granule per 128 bytes keeps
+// strided butterfly accesses spread over the banks while every 128-byte
+// chunk of a vector stays 16-byte aligned (a bulk-copy destination)
+template <class E> struct PadShift {
+  static constexpr int v = sizeof(E) == 4 ? 5 : (sizeof(E) == 8 ? 4 : 3);
+  static constexpr int mul = 16 / (int)sizeof(E);
+};
 
 template <class E> __host__ __device__ __forceinline__ int pidx(int i) {
-  return i + (i >> PadShift<E>::v);
+  return i + PadShift<E>::mul * (i >> PadShift<E>::v);
 }
 
 // ---------------------------------------------------------------- arithmetic
@@ -99,6 +238,17 @@ __device__ __forceinline__ double2 mulv(double2 a, double2 b, bool c) {
   return c ? cmulc(a, b) : cmul(a, b);
 }
 
+__device__ __forceinline__ df mulv(df a, df b, bool) { return a * b; }
+__device__ __forceinline__ dfc mulv(dfc a, dfc b, bool c) {
+  return c ? cmulc(a, b) : cmul(a, b);
+}
+__device__ __forceinline__ df conjv(df a) { return a; }
+__device__ __forceinline__ dfc conjv(dfc a) { return dfc{a.x, -a.y}; }
+__device__ __forceinline__ df addv(df a, df b) { return a + b; }
+__device__ __forceinline__ dfc addv(dfc a, dfc b) { return a + b; }
+__device__ __forceinline__ df subv(df a, df b) { return a - b; }
+__device__ __forceinline__ dfc subv(dfc a, dfc b) { return a - b; }
+
 __device__ __forceinline__ float conjv(float a) { return a; }
 __device__ __forceinline__ double conjv(double a) { return a; }
 __device__ __forceinline__ i64 conjv(i64 a) { return a; }
@@ -118,6 +268,35 @@ template <> __device__ __forceinline__ float2 zero<float2>() {
 }
 template <> __device__ __forceinline__ double2 zero<double2>() {
   return make_double2(0., 0.);
+}
+template <> __device__ __forceinline__ df zero<df>() { return df(0.f, 0.f); }
+template <> __device__ __forceinline__ dfc zero<dfc>() {
+  return dfc{df(0.f, 0.f), df(0.f, 0.f)};
+}
+
+// a (complex) scalar given in double precision, in the element type E;
+// for double-float types this is the host-free integer split
+template <class E> __device__ __forceinline__ E scalar_of(double re, double im);
+template <> __device__ __forceinline__ float scalar_of<float>(double re, double) {
+  return (float)re;
+}
+template <> __device__ __forceinline__ double scalar_of<double>(double re, double) {
+  return re;
+}
+template <> __device__ __forceinline__ i64 scalar_of<i64>(double re, double) {
+  return (i64)re;
+}
+template <> __device__ __forceinline__ float2 scalar_of<float2>(double re, double im) {
+  return make_float2((float)re, (float)im);
+}
+template <> __device__ __forceinline__ double2 scalar_of<double2>(double re, double im) {
+  return make_double2(re, im);
+}
+template <> __device__ __forceinline__ df scalar_of<df>(double re, double) {
+  return d2df(re);
+}
+template <> __device__ __forceinline__ dfc scalar_of<dfc>(double re, double im) {
+  return dfc{d2df(re), d2df(im)};
 }
 
 __device__ __forceinline__ float addv(float a, float b) { return a + b; }
@@ -203,12 +382,23 @@ __device__ __forceinline__ double2 from_wide<double2>(const Wide &w) {
   return make_double2(w.re, w.im);
 }
 
+template <> __device__ __forceinline__ df from_wide<df>(const Wide &w) {
+  return d2df(w.re);
+}
+template <> __device__ __forceinline__ dfc from_wide<dfc>(const Wide &w) {
+  return dfc{d2df(w.re), d2df(w.im)};
+}
+
 // Load element idx of a buffer of element type `type` as E.  The common case
 // (buffer already in the compute type) is a single typed load.
 template <class E>
 __device__ __forceinline__ E load_as(const void *p, int type, i64 idx) {
-  if (type == Tr<E>::code) return ((const E *)p)[idx];
-  return from_wide<E>(load_wide(p, type, idx));
+  if constexpr (Emu<E>::v) {
+    return from_wide<E>(load_wide(p, type, idx));
+  } else {
+    if (type == Tr<E>::code) return ((const E *)p)[idx];
+    return from_wide<E>(load_wide(p, type, idx));
+  }
 }
 
 __device__ __forceinline__ void split(float v, double &re, double &im) {
@@ -231,13 +421,71 @@ __device__ __forceinline__ void split(double2 v, double &re, double &im) {
   re = v.x;
   im = v.y;
 }
+// exponent field of a double (0 for zero / subnormal)
+__device__ __forceinline__ int dexp(double d) {
+  return (int)(((unsigned long long)__double_as_longlong(d) >> 52) & 0x7FF);
+}
+// d * 2^-s by exponent arithmetic (results below the normal range flush to
+// zero, above it saturate to infinity)
+__device__ __forceinline__ double dscale(double d, int s) {
+  if (s == 0) return d;
+  unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0 || ex == 0x7FF) return d;
+  const int ne = ex - s;
+  const unsigned long long sg = b & 0x8000000000000000ull;
+  if (ne <= 0) return __longlong_as_double((long long)sg);
+  if (ne >= 0x7FF)
+    return __longlong_as_double((long long)(sg | 0x7FF0000000000000ull));
+  b = (b & ~(0x7FFull << 52)) | ((unsigned long long)ne << 52);
+  return __longlong_as_double((long long)b);
+}
+
+// (double-float values carry their vector's power-of-two scale s)
+__device__ __forceinline__ void split(df v, double &re, double &im,
+                                      int s = 0) {
+  re = dscale(df2d(v), -s);
+  im = 0.;
+}
+__device__ __forceinline__ void split(dfc v, double &re, double &im,
+                                      int s = 0) {
+  re = dscale(df2d(v.x), -s);
+  im = dscale(df2d(v.y), -s);
+}
+
+// in-place conversions of a double-float tile element and its float64 /
+// complex128 bit pattern (same size)
+// (s: power-of-two scale of the vector, removed on load, restored on store)
+__device__ __forceinline__ int raw_exp(df raw) {
+  return dexp(*reinterpret_cast<const double *>(&raw));
+}
+__device__ __forceinline__ int raw_exp(dfc raw) {
+  const double2 d = *reinterpret_cast<const double2 *>(&raw);
+  const int a = dexp(d.x), b = dexp(d.y);
+  return a > b ? a : b;
+}
+__device__ __forceinline__ df from_bits(df raw, int s) {
+  return d2df(dscale(*reinterpret_cast<const double *>(&raw), s));
+}
+__device__ __forceinline__ dfc from_bits(dfc raw, int s) {
+  const double2 d = *reinterpret_cast<const double2 *>(&raw);
+  return dfc{d2df(dscale(d.x, s)), d2df(dscale(d.y, s))};
+}
+__device__ __forceinline__ df to_bits(df v, int s) {
+  const double d = dscale(df2d(v), -s);
+  return *reinterpret_cast<const df *>(&d);
+}
+__device__ __forceinline__ dfc to_bits(dfc v, int s) {
+  const double2 d = make_double2(dscale(df2d(v.x), -s), dscale(df2d(v.y), -s));
+  return *reinterpret_cast<const dfc *>(&d);
+}
 
 // Store v (compute type E) into a buffer of element type `type`, optionally
 // adding to what is there.
 template <class E>
 __device__ __forceinline__ void store_as(void *p, int type, i64 idx, E v,
-                                         bool acc) {
-  if (type == Tr<E>::code) {
+                                         bool acc, int scale = 0) {
+  if (!Emu<E>::v && type == Tr<E>::code) {
     E *q = (E *)p + idx;
     *q = acc ? addv(*q, v) : v;
     return;
@@ -266,7 +514,8 @@ __device__ __forceinline__ void store_as(void *p, int type, i64 idx, E v,
     }
   }
   double re, im;
-  split(v, re, im);
+  if constexpr (Emu<E>::v) split(v, re, im, scale);
+  else split(v, re, im);
   switch (type) {
     case FM_F32: {
       float *q = (float *)p + idx;

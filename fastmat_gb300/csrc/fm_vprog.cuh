@@ -102,8 +102,8 @@ template <class E> struct Ept {
 template <class C> __device__ __forceinline__ C rot90(C a, int sign) {
   // a * (i * sign)
   C r;
-  r.x = -sign * a.y;
-  r.y = sign * a.x;
+  r.x = smul(-sign, a.y);
+  r.y = smul(sign, a.x);
   return r;
 }
 
@@ -133,12 +133,12 @@ template <class C> __device__ __forceinline__ void dft8(C *v, int sign) {
   }
   // b_k *= exp(sign 2 pi i k / 8)
   C t;
-  t.x = h * (b[1].x - sign * b[1].y);
-  t.y = h * (b[1].y + sign * b[1].x);
+  t.x = h * (b[1].x - smul(sign, b[1].y));
+  t.y = h * (b[1].y + smul(sign, b[1].x));
   b[1] = t;
   b[2] = rot90(b[2], sign);
-  t.x = h * (-b[3].x - sign * b[3].y);
-  t.y = h * (-b[3].y + sign * b[3].x);
+  t.x = h * (-b[3].x - smul(sign, b[3].y));
+  t.y = h * (-b[3].y + smul(sign, b[3].x));
   b[3] = t;
   dft4(a, sign);
   dft4(b, sign);
@@ -163,7 +163,7 @@ template <class C> __device__ __forceinline__ void dft16(C *v, int sign) {
   for (int k = 0; k < 8; ++k) {
     a[k] = v[k] + v[k + 8];
     C d = v[k] - v[k + 8];
-    const R c = cs[k], s = sign * sn[k];
+    const R c = cs[k], s = smul(sign, sn[k]);
     b[k].x = d.x * c - d.y * s;
     b[k].y = d.x * s + d.y * c;
   }
@@ -178,14 +178,15 @@ template <class C> __device__ __forceinline__ void dft16(C *v, int sign) {
 
 template <class C> __device__ __forceinline__ void dft3(C *v, int sign) {
   typedef typename Tr<C>::R R;
-  const R c = (R)-0.5, s = (R)(sign * 0.8660254037844386);
+  const R c = (R)-0.5, s0 = (R)0.8660254037844386;
+  const R s = sign < 0 ? -s0 : s0;
   C t = v[1] + v[2], d = v[1] - v[2];
   C y0 = v[0] + t;
   C m;
   m.x = v[0].x + c * t.x;
   m.y = v[0].y + c * t.y;
   C r;
-  r.x = -s * d.y;
+  r.x = -(s * d.y);
   r.y = s * d.x;
   v[0] = y0;
   v[1] = m + r;
@@ -199,9 +200,9 @@ template <class C>
 __device__ __forceinline__ C pair_out(C a, C b, int sign, bool plus) {
   // a + i*sign*b  (plus) or  a - i*sign*b
   C r;
-  const typename Tr<C>::R sb = plus ? sign : -sign;
-  r.x = a.x - sb * b.y;
-  r.y = a.y + sb * b.x;
+  const int sb = plus ? sign : -sign;
+  r.x = a.x - smul(sb, b.y);
+  r.y = a.y + smul(sb, b.x);
   return r;
 }
 
@@ -293,7 +294,8 @@ __device__ __forceinline__ C twc(C x, int sign) {
   } else if constexpr (idx == 4) {
     return rot90(x, sign);  // * (i sign)
   } else {
-    const R c = (R)kCos16(idx), sn = (R)(sign * kSin16(idx));
+    const R c = (R)kCos16(idx), sp = (R)kSin16(idx);
+    const R sn = sign < 0 ? -sp : sp;
     C r;
     r.x = x.x * c - x.y * sn;
     r.y = x.x * sn + x.y * c;
@@ -399,11 +401,12 @@ __device__ __forceinline__ E *vbase(E *sm, int b, int Lp) {
 // natural order; with opposite signs the two are inverse up to the factor L.
 // Each work item reads and writes the same R positions, so a stage needs one
 // barrier and holds only R values per thread.
-template <int R, bool DIT, int LAY, class C>
+template <int R, bool DIT, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
-                                          int Mprev, int sign,
+                                          int Mprev,
                                           const C *__restrict__ tw, int tid,
                                           int T) {
+  constexpr int sign = SG;
   const int M = Mprev / R;
   const int nw = Lf / R;
   const int total = B * nw;
@@ -465,29 +468,45 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
   __syncthreads();
 }
 
+template <bool DIT, int CLS, int LAY, int SG, class C>
+__device__ __forceinline__ void fft_stage_s(int R, C *sm, int Lp, int B,
+                                            int Lf, int Mprev, const C *tw,
+                                            int tid, int T) {
+  switch (R) {
+    case 2: fft_stage<2, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
+    case 4: fft_stage<4, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
+    case 8: fft_stage<8, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
+    case 16:
+      // double-float vectors of 16 elements do not fit the register budget
+      if constexpr (!Emu<C>::v)
+        fft_stage<16, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      break;
+    case 3:
+      if constexpr (CLS != 1)
+        fft_stage<3, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      break;
+    case 5:
+      if constexpr (CLS != 1)
+        fft_stage<5, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      break;
+    case 7:
+      if constexpr (CLS != 1)
+        fft_stage<7, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      break;
+    default: break;
+  }
+}
+
+// the transform sign is a template parameter of the stages, so rotations
+// by +-i and conjugated twiddles cost no run-time selects
 template <bool DIT, int CLS, int LAY, class C>
 __device__ __forceinline__ void fft_stage_r(int R, C *sm, int Lp, int B,
                                             int Lf, int Mprev, int sign,
                                             const C *tw, int tid, int T) {
-  switch (R) {
-    case 2: fft_stage<2, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
-    case 4: fft_stage<4, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
-    case 8: fft_stage<8, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
-    case 16: fft_stage<16, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T); break;
-    case 3:
-      if constexpr (CLS != 1)
-        fft_stage<3, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
-      break;
-    case 5:
-      if constexpr (CLS != 1)
-        fft_stage<5, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
-      break;
-    case 7:
-      if constexpr (CLS != 1)
-        fft_stage<7, DIT, LAY>(sm, Lp, B, Lf, Mprev, sign, tw, tid, T);
-      break;
-    default: break;
-  }
+  if (sign < 0)
+    fft_stage_s<DIT, CLS, LAY, -1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T);
+  else
+    fft_stage_s<DIT, CLS, LAY, +1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T);
 }
 
 template <class C, int CLS, int LAY>
@@ -662,7 +681,7 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
         *e = mulv(*e, m, op.sign != 0);
         break;
       }
-      case OP_SCALE: *e = scalev(*e, op.sre, op.sim); break;
+      case OP_SCALE: *e = mulv(*e, scalar_of<E>(op.sre, op.sim), false); break;
       case OP_CONJ: *e = conjv(*e); break;
       case OP_TW: {
         if constexpr (Tr<E>::cplx) {
@@ -795,6 +814,23 @@ __device__ __forceinline__ void bulk_wait_all() {
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
+// 1-D bulk copies (cp.async.bulk): 16-byte aligned, multiple of 16 bytes
+__device__ __forceinline__ void bulk_load(unsigned dst, const void *src,
+                                          unsigned bytes, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];\n" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, unsigned src,
+                                           unsigned bytes) {
+  asm volatile(
+      "cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(
+          dst),
+      "r"(src), "r"(bytes)
+      : "memory");
+}
 
 // bytes of one tile buffer (B vectors of Lp elements), 128-byte aligned
 __host__ __device__ __forceinline__ size_t tile_bytes(int B, int Lp,
@@ -807,7 +843,7 @@ __host__ __device__ __forceinline__ size_t tile_bytes(int B, int Lp,
 __host__ __device__ __forceinline__ size_t launch_smem(int B, int Lp, int esz,
                                                        int nbuf) {
   return nbuf * tile_bytes(B, Lp, esz) + 8 * (size_t)nbuf +
-         (size_t)B * (nbuf * sizeof(VInfo) + 8);
+         (size_t)B * (nbuf * sizeof(VInfo) + 8 + 4);
 }
 
 // per-vector addressing of tile `tile` (vector indices below 2^31)
@@ -871,6 +907,109 @@ __device__ __forceinline__ void tma_issue_store(const Step &p, const E *sm,
     tma_store_4d(&p.tm_out, smem_addr(sm + (size_t)j0 * p.B), c0 * p.elem_k,
                  j0, a, m);
   bulk_commit();
+}
+
+// Hardware copies of a whole tile.  Element-major tiles: TMA boxes issued by
+// one thread.  Vector-major tiles of contiguous vectors: one 1-D bulk copy
+// per 128-byte chunk of every vector, spread over the threads, into the
+// padded layout (each chunk is contiguous and 16-byte aligned there).
+template <class E, int LAY>
+__device__ __forceinline__ void issue_load(const Step &p, E *sm, unsigned bar,
+                                           i64 tile, const FDiv &dV, i64 nvec,
+                                           int tid, int T) {
+  if constexpr (LAY == 1) {
+    if (tid == 0) tma_issue_load<E>(p, sm, bar, tile);
+  } else {
+    constexpr int CH = 128 / (int)sizeof(E);
+    const int nch = (p.in_len + CH - 1) / CH;
+    const i64 gv0 = tile * p.B;
+    const i64 nv = nvec - gv0 < p.B ? nvec - gv0 : p.B;
+    if (tid == 0)
+      mbar_expect_tx(bar, (unsigned)((size_t)nv * p.in_len * sizeof(E)));
+    const E *src = (const E *)p.src;
+    for (int c = tid; c < nv * nch; c += T) {
+      const int b = c / nch, k = c - b * nch;
+      const unsigned g = (unsigned)(gv0 + b);
+      const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
+      const i64 off = (i64)m * p.ld_src + (i64)v * p.vin.n + (i64)k * CH;
+      const int cnt = p.in_len - k * CH < CH ? p.in_len - k * CH : CH;
+      bulk_load(smem_addr(sm + b * p.Lp + pidx<E>(k * CH)), src + off,
+                (unsigned)(cnt * sizeof(E)), bar);
+    }
+  }
+}
+
+template <class E, int LAY>
+__device__ __forceinline__ void issue_store(const Step &p, const E *sm,
+                                            i64 tile, const FDiv &dV,
+                                            i64 nvec, int tid, int T) {
+  if constexpr (LAY == 1) {
+    if (tid == 0) tma_issue_store<E>(p, sm, tile);
+  } else {
+    constexpr int CH = 128 / (int)sizeof(E);
+    const int nch = (p.out_len + CH - 1) / CH;
+    const i64 gv0 = tile * p.B;
+    const i64 nv = nvec - gv0 < p.B ? nvec - gv0 : p.B;
+    E *dst = (E *)p.dst;
+    fence_async_smem();
+    bool any = false;
+    for (int c = tid; c < nv * nch; c += T) {
+      const int b = c / nch, k = c - b * nch;
+      const unsigned g = (unsigned)(gv0 + b);
+      const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
+      const i64 off = (i64)m * p.ld_dst + (i64)v * p.vout.n + (i64)k * CH;
+      const int cnt = p.out_len - k * CH < CH ? p.out_len - k * CH : CH;
+      bulk_store(dst + off, smem_addr(sm + b * p.Lp + pidx<E>(k * CH)),
+                 (unsigned)(cnt * sizeof(E)));
+      any = true;
+    }
+    if (any) bulk_commit();
+  }
+}
+
+// vector-major tiles before a bulk store: reorder (out_pos), post-multiply,
+// scale, conjugate and (double-float) convert in shared memory
+template <class E>
+__device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
+                                               const VInfo *vi,
+                                               const int *sexp, int tid,
+                                               int T) {
+  const int B = p.B, Lp = p.Lp, n = p.out_len;
+  const int total = B * n;
+  if (p.out_pos) {
+    constexpr int MB = Ept<E>::v;
+    E v[MB];
+    {
+      Walk w(tid, n, T);
+#pragma unroll
+      for (int i = 0; i < MB; ++i, w.next())
+        if (tid + i * T < total)
+          v[i] = sm[w.b * Lp + pidx<E>(p.out_pos[w.j])];
+    }
+    __syncthreads();
+    {
+      Walk w(tid, n, T);
+#pragma unroll
+      for (int i = 0; i < MB; ++i, w.next())
+        if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
+    }
+    __syncthreads();
+  }
+  const bool any = p.post || p.has_scale || p.conj_out || Emu<E>::v;
+  if (!any) return;
+  Walk w(tid, n, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    const int b = w.b, j = w.j;
+    E *e = sm + b * Lp + pidx<E>(j);
+    E val = *e;
+    if (p.post && vi[b].rb_out >= 0)
+      val = mulv(val, ((const E *)p.post)[vi[b].rb_out + j], false);
+    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
+    if (p.conj_out) val = conjv(val);
+    if constexpr (Emu<E>::v) val = to_bits(val, sexp[b]);
+    *e = val;
+  }
+  __syncthreads();
 }
 
 // asynchronous per-thread load of a tile whose source already has the
@@ -1008,7 +1147,7 @@ __device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
       const i64 rb = vi[b].rb_out;
       if (rb >= 0) val = mulv(val, ((const E *)p.post)[rb + (i64)j * cc], false);
     }
-    if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
     if (p.conj_out) val = conjv(val);
     sm[f] = val;
   }
@@ -1017,7 +1156,8 @@ __device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
 
 template <class E, int LAY>
 __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
-                                           const VInfo *vi, int tid, int T) {
+                                           const VInfo *vi, const int *sexp,
+                                           int tid, int T) {
   const int B = p.B, Lp = p.Lp;
   const bool acc = p.accumulate != 0;
   if constexpr (LAY == 0) {
@@ -1030,9 +1170,10 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
         const i64 j = p.map_out[i];
         E val = j < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)j)];
         if (j >= 0 && p.post) val = mulv(val, ((const E *)p.post)[j], false);
-        if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+        if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
         if (p.conj_out) val = conjv(val);
-        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + i, val, acc);
+        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + i, val, acc,
+                    Emu<E>::v ? sexp[b] : 0);
       }
       return;
     }
@@ -1059,13 +1200,81 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
     E val = vbase<E, LAY>(const_cast<E *>(sm), b, Lp)
         [jx<E, LAY>(p.out_pos ? p.out_pos[j] : j, B)];
     if (p.post) val = mulv(val, ((const E *)p.post)[r], false);
-    if (p.has_scale) val = scalev(val, p.scale_re, p.scale_im);
+    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
     if (p.conj_out) val = conjv(val);
-    if (p.dst_type == Tr<E>::code && !acc)
-      ((E *)p.dst)[vi[b].col_dst + drow] = val;
-    else
-      store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc);
+    if constexpr (Emu<E>::v) {
+      if (p.dst_type == Tr<E>::code && !acc)
+        ((E *)p.dst)[vi[b].col_dst + drow] = to_bits(val, sexp[b]);
+      else
+        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc,
+                    sexp[b]);
+    } else {
+      if (p.dst_type == Tr<E>::code && !acc)
+        ((E *)p.dst)[vi[b].col_dst + drow] = val;
+      else
+        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc);
+    }
   }
+}
+
+// ---- double-float tiles: the tile arrives as float64 / complex128 bits;
+// each vector is normalised by the power of two of its largest exponent
+// (exact) and split into double-floats in place; the store path reverses it
+template <class E, int LAY>
+__device__ __forceinline__ void emu_in(const Step &p, E *sm, const VInfo *vi,
+                                       int *sexp, int tid, int T) {
+  const int B = p.B, L = p.L, Lp = p.Lp;
+  const int total = B * L;
+  const int lgB = __ffs(B) - 1;
+  for (int b = tid; b < B; b += T) sexp[b] = 0;
+  __syncthreads();
+  {
+    // per-thread maximum over the run of elements of one vector, one
+    // shared-memory atomic per run
+    Walk w(tid, L, T);
+    int cb = -1, cmax = 0;
+    for (int f = tid; f < total; f += T, w.next()) {
+      int b, j;
+      if constexpr (LAY == 1) {
+        b = f & (B - 1);
+        j = f >> lgB;
+      } else {
+        b = w.b;
+        j = w.j;
+      }
+      if (b != cb) {
+        if (cb >= 0 && cmax > 0) atomicMax(sexp + cb, cmax);
+        cb = b;
+        cmax = 0;
+      }
+      const int e = raw_exp(vbase<E, LAY>(sm, b, Lp)[jx<E, LAY>(j, B)]);
+      cmax = e > cmax ? e : cmax;
+    }
+    if (cb >= 0 && cmax > 0) atomicMax(sexp + cb, cmax);
+  }
+  __syncthreads();
+  for (int b = tid; b < B; b += T) sexp[b] = sexp[b] > 0 ? sexp[b] - 1023 : 0;
+  __syncthreads();
+  Walk w(tid, L, T);
+  for (int f = tid; f < total; f += T, w.next()) {
+    int b, j;
+    if constexpr (LAY == 1) {
+      b = f & (B - 1);
+      j = f >> lgB;
+    } else {
+      b = w.b;
+      j = w.j;
+    }
+    E *e = vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B);
+    *e = from_bits(*e, sexp[b]);
+  }
+}
+
+template <class E>
+__device__ __forceinline__ void emu_out_em(const Step &p, E *sm,
+                                          const int *sexp, int tid, int T) {
+  const int total = p.B * p.L;
+  for (int f = tid; f < total; f += T) sm[f] = to_bits(sm[f], sexp[f & (p.B - 1)]);
 }
 
 template <class E, int CLS, int LAY>
@@ -1130,14 +1339,15 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
       reinterpret_cast<unsigned long long *>(fm_smem + NB * tb);
   VInfo *const vi0 = reinterpret_cast<VInfo *>(bars + NB);
   i64 *sq = reinterpret_cast<i64 *>(vi0 + NB * B);
+  int *sexp = reinterpret_cast<int *>(sq + B);  // per-vector scale (emu)
   auto buf = [&](int k) { return reinterpret_cast<E *>(fm_smem + k * tb); };
   auto vis = [&](int k) { return vi0 + k * B; };
   const i64 nvec = p.V * p.num_cols;
   const i64 ntiles = (nvec + B - 1) / B;
   const FDiv dV((unsigned)p.V), dci((unsigned)p.vin.Cc),
       dco((unsigned)p.vout.Cc);
-  const bool tma_in = LAY == 1 && p.tma_in;
-  const bool tma_out = LAY == 1 && p.tma_out;
+  const bool tma_in = p.tma_in != 0;    // hardware copies into the ring
+  const bool tma_out = p.tma_out != 0;  // hardware copies out of the tile
   const bool async_in = tma_in || (p.src_type == Tr<E>::code && !p.map_in);
   const bool fixup = p.conj_in || p.pre;
   const i64 G = gridDim.x;
@@ -1158,7 +1368,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
       if (t < ntiles) {
         setup_tile(p, vis(k), t, dV, dci, dco, nvec, tid, T);
         if (tma_in) {
-          if (tid == 0) tma_issue_load<E>(p, buf(k), smem_addr(bars + k), t);
+          issue_load<E, LAY>(p, buf(k), smem_addr(bars + k), t, dV, nvec, tid,
+                             T);
         } else {
           __syncthreads();
           load_async<E, LAY>(p, buf(k), vis(k), tid, T);
@@ -1173,9 +1384,9 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
   while (tile < ntiles) {
     E *sm = buf(cur);
     VInfo *vi = vis(cur);
-    // per-thread loads refill buffers that a TMA store may still be
+    // per-thread loads refill buffers that a bulk store may still be
     // reading: wait for those reads (a barrier follows before any refill)
-    if (tma_out && !tma_in && tid == 0) bulk_wait_read<0>();
+    if (tma_out && !tma_in) bulk_wait_read<0>();
     if (async_in) {
       if (!tma_in) {
         const i64 ahead = tile + (NB - 1) * G;
@@ -1199,12 +1410,18 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
         phase_bits ^= 1u << cur;
       }
       __syncthreads();
+      if constexpr (Emu<E>::v) {
+        emu_in<E, LAY>(p, sm, vi, sexp, tid, T);
+        __syncthreads();
+      }
       if (fixup) {
         load_fixup<E, LAY>(p, sm, vi, tid, T);
         __syncthreads();
       }
     } else {
       setup_tile(p, vi, tile, dV, dci, dco, nvec, tid, T);
+      if constexpr (Emu<E>::v)
+        for (int b = tid; b < B; b += T) sexp[b] = 0;
       __syncthreads();
       load_general<E, LAY>(p, sm, vi, tid, T);
       __syncthreads();
@@ -1213,10 +1430,22 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
     run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T);
 
     if (tma_out) {
-      store_fixup_em<E>(p, sm, vi, tid, T);
-      if (tid == 0) tma_issue_store<E>(p, sm, tile);
+      if constexpr (LAY == 1) {
+        store_fixup_em<E>(p, sm, vi, tid, T);
+        if constexpr (Emu<E>::v) {
+          emu_out_em<E>(p, sm, sexp, tid, T);
+          __syncthreads();
+        }
+      } else {
+        store_fixup_vm<E>(p, sm, vi, sexp, tid, T);
+      }
+      // every writer orders its shared-memory writes before the bulk /
+      // TMA reads of the store, then the issuing threads start it
+      fence_async_smem();
+      __syncthreads();
+      issue_store<E, LAY>(p, sm, tile, dV, nvec, tid, T);
     } else {
-      store_tile<E, LAY>(p, sm, vi, tid, T);
+      store_tile<E, LAY>(p, sm, vi, sexp, tid, T);
     }
     if (tma_in) {
       // refill the buffer freed one iteration ago (tile - G) with the tile
@@ -1224,14 +1453,15 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
       const i64 ahead = tile + (NB - 1) * G;
       int slot = cur + NB - 1;
       if (slot >= NB) slot -= NB;
+      // every thread that issued bulk stores waits until the older ones
+      // have been read out of shared memory
+      if (tma_out) bulk_wait_read<1>();
+      fence_async_smem();
       __syncthreads();
       if (ahead < ntiles) {
         setup_tile(p, vis(slot), ahead, dV, dci, dco, nvec, tid, T);
-        if (tid == 0) {
-          if (tma_out) bulk_wait_read<1>();
-          fence_async_smem();
-          tma_issue_load<E>(p, buf(slot), smem_addr(bars + slot), ahead);
-        }
+        issue_load<E, LAY>(p, buf(slot), smem_addr(bars + slot), ahead, dV,
+                           nvec, tid, T);
       }
     }
     __syncthreads();
@@ -1249,7 +1479,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
         mbar_wait(smem_addr(bars + k), (phase_bits >> k) & 1u, FM_WAIT_LIMIT);
     }
   }
-  if (tma_out && tid == 0) bulk_wait_all();
+  if (tma_out) bulk_wait_all();
   if (!tma_in) cp_async_wait<0>();
 }
 

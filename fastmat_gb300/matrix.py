@@ -92,10 +92,21 @@ def _numpy_dtype(tdt):
     raise TypeError("unsupported tensor dtype %s" % tdt)
 
 
-def _compute_code(out_dtype):
+def _compute_code(out_dtype, precision='native'):
+    """Element type a plan computes in for a given output type.
+
+    float64 / complex128 results are computed in double-float arithmetic
+    (pairs of float32, ~2^-48 relative precision) unless
+    ``precision='fp64'`` asks for the FP64 pipe; integer results in int64.
+    """
     dt = np.dtype(out_dtype)
     if dt.kind in 'iub':
         return _native.FM_I64
+    if precision != 'fp64':
+        if dt == np.complex128:
+            return _native.FM_C128_DF
+        if dt == np.float64:
+            return _native.FM_F64_DF
     return _native.DTYPE_CODE[dt]
 
 
@@ -105,8 +116,11 @@ class Matrix:
     ``Matrix(array)`` wraps a dense 2-D array (fastmat/Matrix.pyx:1468);
     subclasses define structured operators.  Options (keyword arguments)
     follow fastmat: ``minType`` (minimum internal type) and
-    ``widenInputDatatype``; ``precision='fp32'`` is this package's opt-in
-    reduced-precision form (float32 / complex64 arithmetic and output).
+    ``widenInputDatatype``.  ``precision`` selects how floating-point work
+    is done: ``'native'`` (default: float64 / complex128 results computed in
+    double-float arithmetic on the FP32 pipes), ``'fp64'`` (the FP64 pipe)
+    or ``'fp32'`` (opt-in reduced precision: float32 / complex64 arithmetic
+    and output).
     """
 
     _array = None
@@ -250,7 +264,7 @@ class Matrix:
 
     def plan(self, out_dtype=np.complex128):
         """The native plan computing in the type of ``out_dtype``."""
-        code = _compute_code(out_dtype)
+        code = _compute_code(out_dtype, self._precision)
         p = self._plans.get(code)
         if p is None:
             b = _Builder()
@@ -258,6 +272,16 @@ class Matrix:
             p = _native.Plan(b.nodes, b.children, root, code, b.keep)
             self._plans[code] = p
         return p
+
+    def autotune(self, num_cols=1, out_dtype=None, cache=True):
+        """Pick the tile shape of every GPU launch of this operator by
+        timing the candidates (see fm_plan_autotune) for `num_cols`
+        columns; the choice is cached on disk per device and plan."""
+        from . import tuning
+        if out_dtype is None:
+            out_dtype = self._output_dtype(np.complex128 if T.is_complex(
+                self.dtype) else np.float64)
+        return tuning.autotune(self.plan(out_dtype), num_cols, cache)
 
     def forward(self, arrX):
         """y = A x.  1-D or 2-D numpy arrays or CUDA torch tensors."""

@@ -100,6 +100,13 @@ typedef struct fm_node {
     double scalar_re, scalar_im;
 } fm_node;
 
+/* compute types accepted by fm_plan_create besides the FM_* element types:
+ * float64 / complex128 data computed in double-float arithmetic (pairs of
+ * float32, about 2^-48 relative precision) on the FP32 pipes, which this GPU
+ * runs far faster than its FP64 pipe; buffers keep float64 / complex128 */
+#define FM_F64_DF 16
+#define FM_C128_DF 17
+
 /* plan precisions */
 #define FM_PREC_NATIVE 0  /* compute in the operator/input promoted type     */
 #define FM_PREC_FP32 1    /* opt-in: float32 / complex64 arithmetic          */
@@ -178,6 +185,26 @@ int fm_execute_host(fm_plan *plan, int32_t direction,
                     const void *x, int32_t x_type, int64_t ld_x,
                     void *y, int32_t y_type, int64_t ld_y,
                     int64_t num_cols);
+
+/* Tile shape of launch `launch` of a direction: vectors per tile and the
+ * depth (2..4) of its copy ring; fm_plan_set_tile returns FM_ERR_VALUE for
+ * an infeasible request and leaves the launch unchanged.  layout: 0 vector-
+ * major, 1 element-major (TMA boxes).  The reference has no counterpart. */
+int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,
+                     int32_t vectors_per_tile, int32_t nbuf);
+int fm_plan_get_tile(const fm_plan *plan, int32_t direction, int32_t launch,
+                     int32_t *vectors_per_tile, int32_t *nbuf,
+                     int32_t *layout);
+
+/* Autotuner: for every launch of `direction`, time each feasible tile
+ * shape on temporary buffers shaped like the launch's operands for
+ * `num_cols` columns (a sample of at most ~512 MiB per operand) and keep the
+ * fastest.  Synchronous; allocates temporaries.  The choices can be read
+ * back with fm_plan_get_tile and replayed with fm_plan_set_tile (the Python
+ * layer caches them on disk).  The reference has no counterpart (its
+ * calibration fits CPU runtime models, fastmat/core/calibration.py). */
+int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
+                     void *stream);
 
 /* Report (and clear) a failure that kernels of this plan recorded on the
  * device since the last check: FM_ERR_TIMEOUT if a bounded wait for a tile
