@@ -73,7 +73,7 @@ EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
            'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
            'fm_plan_set_tile', 'fm_plan_get_tile', 'fm_plan_autotune',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
-           'fm_last_error', 'fm_version')
+           'fm_reduce_mulconj', 'fm_last_error', 'fm_version')
 
 _lib = None
 _lock = threading.Lock()
@@ -131,6 +131,10 @@ def load(build_if_missing=True):
         lib.fm_plan_get_info.restype = ctypes.c_int
         lib.fm_plan_describe.argtypes = [P, I32, ctypes.c_char_p, I64]
         lib.fm_plan_describe.restype = ctypes.c_int
+        lib.fm_reduce_mulconj.argtypes = [I64, I64, I64, I64, I32, P, I64,
+                                          P, I64, P, ctypes.c_double, P, P,
+                                          I64, P]
+        lib.fm_reduce_mulconj.restype = ctypes.c_int
         lib.fm_last_error.argtypes = []
         lib.fm_last_error.restype = ctypes.c_char_p
         lib.fm_version.argtypes = []
@@ -244,3 +248,11 @@ class Plan:
             except Exception:
                 pass
             self.handle = None
+
+
+def reduce_mulconj(A, n, Cc, num_cols, type_code, u, ld_u, v, ld_v, out,
+                   scale=1.0, d=None, w=None, ld_w=0, stream=None):
+    """fm_reduce_mulconj on device pointers (see include/fmgpu.h)."""
+    lib = load()
+    check(lib.fm_reduce_mulconj(A, n, Cc, num_cols, type_code, u, ld_u, v,
+                                ld_v, out, scale, d, w, ld_w, stream))

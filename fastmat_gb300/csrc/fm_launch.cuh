@@ -24,6 +24,9 @@ cudaError_t launch_dfc(const Step &st, int cls, int lay, int threads,
 cudaError_t launch_i64(const Step &st, int cls, int lay, int threads,
                        size_t smem, i64 grid, cudaStream_t s);
 
+// records the message fm_last_error() returns on the calling thread
+void set_last_error(const char *msg);
+
 // maximum dynamic shared memory a launch may request (GB300: 227 KB / CTA)
 constexpr int kMaxSmem = 227 * 1024;
 

@@ -252,6 +252,8 @@ struct SStep {
   std::vector<fmk::Op> ops;
   int src = -1, dst = -2;  // -1 unit input, -2 unit output, k >= 0 temp k
   const void *pre = nullptr, *post = nullptr;
+  const i64 *map_in = nullptr, *map_out = nullptr;  // gather / scatter
+  int out_mode = 0;
   int conj_in = 0, conj_out = 0;
 };
 
@@ -1147,7 +1149,26 @@ class Planner {
       }
       out.push_back(u);
     }
-    return out;
+    // fold pointwise programs into neighbouring multi-launch units
+    Chain fused;
+    for (size_t i = 0; i < out.size(); ++i) {
+      if (i + 1 < out.size() && out[i + 1].kind == Unit::STEPS) {
+        Unit next = out[i + 1];
+        if (fold_before(out[i], next)) {
+          out[i + 1] = next;
+          continue;
+        }
+      }
+      if (!fused.empty() && fused.back().kind == Unit::STEPS) {
+        Unit prev = fused.back();
+        if (fold_after(prev, out[i])) {
+          fused.back() = prev;
+          continue;
+        }
+      }
+      fused.push_back(out[i]);
+    }
+    return fused;
   }
 
   Chain kron(const NodeRec &r, bool fwd) {
@@ -1295,13 +1316,21 @@ class Planner {
     emit_chunked(u, src, dst, out);
   }
 
-  // y[i] = s * d[i] * cx(x[map[i]]) over chunks of the column
-  void emit_chunked(const Unit &u, int src, int dst, std::vector<LStep> &out) {
-    i64 len = u.n_in;
-    std::vector<i64> map;  // empty: identity
-    std::vector<cd> dv;    // empty: ones
-    cd s(1, 0);
+  // A program made only of pointwise operations and gathers, composed into
+  // y[i] = s * d[i] * cx(x[map[i]]) (map empty: identity, d empty: ones).
+  struct Pointwise {
+    std::vector<i64> map;
+    std::vector<cd> dv;
+    cd s{1, 0};
     bool cx = false;
+    i64 len = 0;
+  };
+
+  bool pointwise(const Unit &u, Pointwise &pw) {
+    if (u.kind != Unit::PROG) return false;
+    i64 len = u.n_in;
+    std::vector<i64> &map = pw.map;
+    std::vector<cd> &dv = pw.dv;
     for (const fmk::Op &o : u.ops) {
       switch (o.kind) {
         case fmk::OP_GATHER: {
@@ -1320,23 +1349,104 @@ class Planner {
           break;
         }
         case fmk::OP_MUL: {
+          if (o.div != 1 || o.mod != 1 || o.stride != 0) return false;
           const std::vector<cd> &v = host_vec_.at(o.ptr);
           if (dv.empty()) dv.assign((size_t)len, cd(1, 0));
           for (i64 i = 0; i < len; ++i)
             dv[i] *= o.sign ? std::conj(v[i]) : v[i];
           break;
         }
-        case fmk::OP_SCALE: s *= cd(o.sre, o.sim); break;
+        case fmk::OP_SCALE: pw.s *= cd(o.sre, o.sim); break;
         case fmk::OP_CONJ:
-          s = std::conj(s);
+          pw.s = std::conj(pw.s);
           for (cd &x : dv) x = std::conj(x);
-          cx = !cx;
+          pw.cx = !pw.cx;
           break;
-        default:
-          fail(FM_ERR_UNSUPPORTED,
-               "long vector program with non-pointwise operations");
+        default: return false;
       }
     }
+    pw.len = len;
+    return true;
+  }
+
+  // Fold a pointwise program that feeds a multi-launch unit into the
+  // loader of its first launch (gather map, conjugation and
+  // pre-multiplication).
+  bool fold_before(const Unit &p, Unit &u) {
+    Pointwise pw;
+    if (!pointwise(p, pw) || u.kind != Unit::STEPS || u.steps.empty())
+      return false;
+    SStep &a = u.steps[0];
+    if (a.src != -1 || a.pre || a.map_in || a.conj_in) return false;
+    for (size_t k = 1; k < u.steps.size(); ++k)
+      if (u.steps[k].src == -1) return false;  // input read again later
+    if (pw.len != u.n_in || a.in_rows != u.n_in) return false;
+    if (pw.s != cd(1, 0)) {
+      if (pw.dv.empty()) pw.dv.assign((size_t)pw.len, cd(1, 0));
+      for (cd &x : pw.dv) x *= pw.s;
+    }
+    if (!pw.map.empty()) a.map_in = upload_map(pw.map);
+    if (!pw.dv.empty()) a.pre = upload(pw.dv);
+    a.conj_in = pw.cx;
+    u.n_in = p.n_in;
+    return true;
+  }
+
+  // Fold a pointwise program that consumes a multi-launch unit's result
+  // into the storer of its last launch (post-multiplication, conjugation,
+  // and a row selection as a scatter through the inverse map).  Only
+  // selections that pick every row at most once can be inverted.
+  bool fold_after(Unit &u, const Unit &p) {
+    Pointwise pw;
+    if (u.kind != Unit::STEPS || u.steps.empty() || !pointwise(p, pw))
+      return false;
+    SStep &c = u.steps.back();
+    if (c.dst != -2 || c.post || c.map_out || c.conj_out) return false;
+    for (size_t k = 0; k + 1 < u.steps.size(); ++k)
+      if (u.steps[k].dst == -2 || u.steps[k].src == -2)
+        return false;  // output buffer also used as working storage
+    if (p.n_in != u.n_out || c.out_rows != u.n_out) return false;
+    std::vector<i64> inv;
+    if (!pw.map.empty()) {
+      inv.assign((size_t)u.n_out, -1);
+      for (size_t i = 0; i < pw.map.size(); ++i) {
+        const i64 j = pw.map[i];
+        if (j < 0 || j >= u.n_out || inv[j] >= 0) return false;
+        inv[j] = (i64)i;
+      }
+    }
+    std::vector<cd> post;
+    if (!pw.dv.empty() || pw.s != cd(1, 0)) {
+      post.assign((size_t)u.n_out, cd(0, 0));
+      for (i64 r = 0; r < u.n_out; ++r) {
+        const i64 i = inv.empty() ? r : inv[r];
+        if (i < 0) continue;
+        cd v = (pw.dv.empty() ? cd(1, 0) : pw.dv[i]) * pw.s;
+        // stored value: conj_out(post * x) = d * cx(x)
+        post[r] = pw.cx ? std::conj(v) : v;
+      }
+    }
+    if (!inv.empty()) {
+      c.map_out = upload_map(inv);
+      c.out_mode = 2;
+    }
+    if (!post.empty()) c.post = upload(post);
+    c.conj_out = pw.cx;
+    u.n_out = pw.len;
+    return true;
+  }
+
+  // y[i] = s * d[i] * cx(x[map[i]]) over chunks of the column
+  void emit_chunked(const Unit &u, int src, int dst, std::vector<LStep> &out) {
+    Pointwise pw;
+    if (!pointwise(u, pw))
+      fail(FM_ERR_UNSUPPORTED,
+           "long vector program with non-pointwise operations");
+    const std::vector<i64> &map = pw.map;
+    std::vector<cd> &dv = pw.dv;
+    const cd s = pw.s;
+    const bool cx = pw.cx;
+    const i64 len = pw.len;
     const i64 n_out = len;
     const i64 Lc = std::min<i64>(2048, std::max<i64>(n_out, 1));
     const i64 nch = (n_out + Lc - 1) / Lc;
@@ -1395,6 +1505,9 @@ class Planner {
       st.V = s.vin.A * s.vin.Cc;
       st.pre = s.pre;
       st.post = s.post;
+      st.map_in = s.map_in;
+      st.map_out = s.map_out;
+      st.out_mode = s.out_mode;
       st.conj_in = s.conj_in;
       st.conj_out = s.conj_out;
       finish(ls, s.ops);
@@ -1734,6 +1847,10 @@ template <class F> int guarded(F f) {
 }  // namespace
 
 // ------------------------------------------------------------ C ABI
+namespace fmk {
+void set_last_error(const char *msg) { g_err = msg ? msg : ""; }
+}  // namespace fmk
+
 extern "C" {
 
 int fm_plan_create(const fm_node *nodes, int32_t num_nodes,

@@ -231,6 +231,31 @@ int fm_plan_get_info(const fm_plan *plan, fm_plan_info *info);
 int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
                      int64_t buf_len);
 
+/* ---- gradients of the differentiable path -----------------------------
+ * Column reduction behind the parameter gradients of a chain of operators.
+ * u, v (and w) are column-major arrays of num_cols columns whose columns are
+ * viewed as 3-D blocks (A, n, Cc): row r = (a * n + j) * Cc + c, the view of
+ * one Kron mode (A = product of the leading factor sizes, Cc = product of
+ * the trailing ones; A = Cc = 1 for a plain vector).  Writes, on `stream`,
+ *
+ *     out[j] = scale * sum_{a < A, c < Cc, k < num_cols} u[r + k ld_u]
+ *                                                        * conj(v[r + k ld_v])
+ *
+ * for j < n (conj is the identity for real types).  With u the upstream
+ * gradient and v the input of a Diag factor this is the gradient of the
+ * diagonal; with u, v in the Fourier domain it is the spectrum of the
+ * circular cross-correlation giving the gradient of a circulant or Toeplitz
+ * defining vector.  If d is not NULL, w[r + k ld_w] = conj(d[j]) * u[...] is
+ * written in the same pass: the adjoint of the Diag factor, fastmat's
+ * Diag backward (fastmat/Diag.pyx:149-167).  type: FM_F32, FM_F64, FM_C64
+ * or FM_C128 for every array.  Deterministic (fixed summation order).
+ * Allocates its partial sums stream-ordered (cudaMallocAsync).  The
+ * reference has no gradients; this has no counterpart there. */
+int fm_reduce_mulconj(int64_t A, int64_t n, int64_t Cc, int64_t num_cols,
+                      int32_t type, const void *u, int64_t ld_u,
+                      const void *v, int64_t ld_v, void *out, double scale,
+                      const void *d, void *w, int64_t ld_w, void *stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char *fm_last_error(void);
 

@@ -174,3 +174,46 @@ def test_fp32_form_error_bound(expr):
     y = A.forward(x)
     assert y.dtype in (np.complex64, np.float32)
     assert fo.rel_err(y, A64.forward(x)) <= 1e-5
+
+
+FOLD_CASES = [
+    # (expression in fg/fo namespace, input rows)
+    ('Product(Fourier(N), Diag(d))', 'N'),
+    ('Product(Diag(d), Fourier(N))', 'N'),
+    ('Product(Partial(Eye(N), rows=rows), Fourier(N), Diag(d))', 'N'),
+    ('Product(Fourier(N), Hermitian(Partial(Eye(N), rows=rows)))', 'R'),
+    ('Product(Fourier(N), Partial(Eye(N), cols=rows))', 'R'),
+    ('Partial(Product(Circulant(c), Diag(d)), rows=rows)', 'N'),
+    ('Conjugate(Product(Diag(d), Fourier(N), Diag(d)))', 'N'),
+    ('Product(Partial(Eye(N), rows=dup), Fourier(N))', 'N'),
+    ('Product(Fourier(N), Permutation(perm), Diag(d), 2.0 - 1j)', 'N'),
+    ('Product(Hadamard(17), Diag(d[:1 << 17]))', 'H'),
+]
+
+
+@pytest.mark.parametrize('expr,rin', FOLD_CASES)
+def test_pointwise_folded_into_long_transforms(expr, rin):
+    """Diagonals, selections, conjugation and scalars next to a multi-launch
+    transform run inside its first / last launch; results must not
+    change."""
+    import fastmat_gb300 as fg
+    N = 1 << 18
+    rng = np.random.default_rng(17)
+    c, d = cplx(rng, N), cplx(rng, N)
+    rows = np.sort(rng.choice(N, N // 4, replace=False))
+    dup = np.concatenate([rows, rows[:100]])
+    perm = rng.permutation(N)
+    ns = dict(N=N, c=c, d=d, rows=rows, dup=dup, perm=perm)
+    gns = dict(ns, **{k: getattr(fg, k) for k in (
+        'Fourier', 'Diag', 'Partial', 'Eye', 'Product', 'Hermitian',
+        'Circulant', 'Conjugate', 'Permutation', 'Hadamard')})
+    ons = dict(ns, Fourier=fo.Fourier, Diag=fo.Diag, Partial=fo.Partial,
+               Eye=fo.Eye, Product=fo.Product, Hermitian=fo.Hermitian,
+               Circulant=fo.Circulant, Conjugate=fo.Conjugate,
+               Permutation=fo.Permutation, Hadamard=fo.Hadamard)
+    op, oop = eval(expr, gns), eval(expr, ons)
+    n_in = {'N': N, 'R': len(rows), 'H': 1 << 17}[rin]
+    x = cplx(rng, n_in, 3)
+    g = cplx(rng, op.numRows, 3)
+    assert fo.rel_err(op.forward(x), oop.forward(x)) <= 1e-12
+    assert fo.rel_err(op.backward(g), oop.backward(g)) <= 1e-12
