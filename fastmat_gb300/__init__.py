@@ -9,13 +9,14 @@ from .matrix import Conjugate, Hermitian, Matrix, Transpose
 from .operators import (Circulant, Diag, Eye, Fourier, Hadamard, Kron,
                         Partial, Permutation, Product, Sum, Toeplitz)
 from . import _native
+from .batch import Batch
 from ._build import build
 
 __version__ = '0.1.0'
 
 __all__ = ['Matrix', 'Hermitian', 'Conjugate', 'Transpose', 'Fourier',
            'Circulant', 'Toeplitz', 'Hadamard', 'Diag', 'Eye', 'Partial',
-           'Permutation', 'Product', 'Sum', 'Kron', 'build']
+           'Permutation', 'Product', 'Sum', 'Kron', 'Batch', 'build']
 
 
 def native_library():

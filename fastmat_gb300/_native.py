@@ -73,6 +73,8 @@ EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
            'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
            'fm_plan_set_tile', 'fm_plan_get_tile', 'fm_plan_autotune',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
+           'fm_batch_create', 'fm_batch_execute', 'fm_batch_execute_graph',
+           'fm_batch_check', 'fm_batch_get_info', 'fm_batch_destroy',
            'fm_reduce_mulconj', 'fm_last_error', 'fm_version')
 
 _lib = None
@@ -131,6 +133,22 @@ def load(build_if_missing=True):
         lib.fm_plan_get_info.restype = ctypes.c_int
         lib.fm_plan_describe.argtypes = [P, I32, ctypes.c_char_p, I64]
         lib.fm_plan_describe.restype = ctypes.c_int
+        PP = ctypes.POINTER(P)
+        PI32 = ctypes.POINTER(I32)
+        PI64 = ctypes.POINTER(I64)
+        lib.fm_batch_create.argtypes = [I32, PP, PI32, PP, PI32, PI64, PP,
+                                        PI32, PI64, PI64, PP]
+        lib.fm_batch_create.restype = ctypes.c_int
+        lib.fm_batch_execute.argtypes = [P, P]
+        lib.fm_batch_execute.restype = ctypes.c_int
+        lib.fm_batch_execute_graph.argtypes = [P, P]
+        lib.fm_batch_execute_graph.restype = ctypes.c_int
+        lib.fm_batch_check.argtypes = [P]
+        lib.fm_batch_check.restype = ctypes.c_int
+        lib.fm_batch_get_info.argtypes = [P, PI64, PI64, PI64]
+        lib.fm_batch_get_info.restype = ctypes.c_int
+        lib.fm_batch_destroy.argtypes = [P]
+        lib.fm_batch_destroy.restype = ctypes.c_int
         lib.fm_reduce_mulconj.argtypes = [I64, I64, I64, I64, I32, P, I64,
                                           P, I64, P, ctypes.c_double, P, P,
                                           I64, P]
@@ -256,3 +274,48 @@ def reduce_mulconj(A, n, Cc, num_cols, type_code, u, ld_u, v, ld_v, out,
     lib = load()
     check(lib.fm_reduce_mulconj(A, n, Cc, num_cols, type_code, u, ld_u, v,
                                 ld_v, out, scale, d, w, ld_w, stream))
+
+
+class BatchHandle:
+    """Owns one native batch (see fm_batch_create)."""
+
+    def __init__(self, plans, directions, xs, x_types, ld_x, ys, y_types,
+                 ld_y, num_cols):
+        lib = load()
+        n = len(plans)
+        P = ctypes.c_void_p
+        arr = lambda t, v: (t * n)(*v)  # noqa: E731
+        handle = ctypes.c_void_p()
+        self._plans = list(plans)   # the batch reads their constants
+        check(lib.fm_batch_create(
+            n, arr(P, [p.handle.value for p in plans]),
+            arr(ctypes.c_int32, directions), arr(P, xs),
+            arr(ctypes.c_int32, x_types), arr(ctypes.c_int64, ld_x),
+            arr(P, ys), arr(ctypes.c_int32, y_types),
+            arr(ctypes.c_int64, ld_y), arr(ctypes.c_int64, num_cols),
+            ctypes.byref(handle)))
+        self.handle = handle
+        self._lib = lib
+
+    def execute(self, stream=None, graph=False):
+        fn = (self._lib.fm_batch_execute_graph if graph
+              else self._lib.fm_batch_execute)
+        check(fn(self.handle, stream))
+
+    def check(self):
+        check(self._lib.fm_batch_check(self.handle))
+
+    def info(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(self._lib.fm_batch_get_info(self.handle, ctypes.byref(a),
+                                          ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                self._lib.fm_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

@@ -24,6 +24,21 @@ cudaError_t launch_dfc(const Step &st, int cls, int lay, int threads,
 cudaError_t launch_i64(const Step &st, int cls, int lay, int threads,
                        size_t smem, i64 grid, cudaStream_t s);
 
+// one batched persistent launch (batch_kernel)
+struct BatchLaunch {
+  int ctype = 0, cls = 0;
+  const Step *steps = nullptr;  // device array, grouped by level
+  const i64 *start = nullptr;   // first tile of every step (+ total)
+  const int *level = nullptr;   // first step of every level (+ count)
+  int nlev = 0;
+  unsigned *bar = nullptr;      // grid-barrier counter, zero at launch
+  int *err = nullptr;
+  int max_B = 1;
+  size_t smem = 0;
+  long long max_level_tiles = 1;
+};
+cudaError_t launch_batch(const BatchLaunch &b, cudaStream_t s);
+
 // records the message fm_last_error() returns on the calling thread
 void set_last_error(const char *msg);
 

@@ -238,6 +238,23 @@ fm_plan::~fm_plan() {
   if (hstream) cudaStreamDestroy(hstream);
 }
 
+struct fm_batch {
+  int device = 0;
+  std::vector<void *> allocs;
+  fmk::BatchLaunch launch;
+  i64 num_steps = 0, total_tiles = 0;
+  int *status = nullptr;  // [0] grid-barrier counter, [1] error word
+  cudaStream_t gstream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~fm_batch();
+};
+
+fm_batch::~fm_batch() {
+  if (exec) cudaGraphExecDestroy(exec);
+  if (gstream) cudaStreamDestroy(gstream);
+  for (void *p : allocs) cudaFree(p);
+}
+
 namespace {
 
 int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
@@ -295,7 +312,8 @@ fmk::Op mkop(int kind, int len) {
 // copy-ring depth and shared memory.  want_B / want_nbuf = 0 picks the
 // heuristic choice; explicit values (the autotuner's candidates) are
 // accepted when feasible.  Returns false if the request cannot be met.
-bool configure(int esz, LStep &ls, int want_B, int want_nbuf) {
+bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
+               bool allow_em = true) {
   fmk::Step &st = ls.st;
   const int L = std::max(st.L, 1);
   const int ept = ls.ept;
@@ -317,7 +335,8 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf) {
   // element-major tiles: strided input and output views whose inner extent
   // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
   // budget allows, never below 16 B), moved by TMA boxes
-  if ((ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 && st.vout.Cc > 1) {
+  if (allow_em && (ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 &&
+      st.vout.Cc > 1) {
     int B = want_B ? want_B : 128 / esz;
     if (!want_B) {
       while (B > 1 && (st.vin.Cc % B || st.vout.Cc % B)) B /= 2;
@@ -2204,6 +2223,256 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
     buf[n] = 0;
     return FM_OK;
   });
+}
+
+int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
+                    const int32_t *directions, const void *const *x,
+                    const int32_t *x_types, const int64_t *ld_x,
+                    void *const *y, const int32_t *y_types,
+                    const int64_t *ld_y, const int64_t *num_cols,
+                    fm_batch **batch) {
+  return guarded([&]() {
+    if (!batch || num_ops < 1 || !plans || !directions || !x || !x_types ||
+        !ld_x || !y || !y_types || !ld_y || !num_cols)
+      fail(FM_ERR_VALUE, "fm_batch_create: NULL argument or no operators");
+    *batch = nullptr;
+    const int ctype = plans[0] ? plans[0]->ctype : -1;
+    if (ctype != FM_C64 && ctype != FM_C128_DF)
+      fail(FM_ERR_UNSUPPORTED, "batches compute in complex64 or complex128 "
+                               "(double-float) only");
+    const int esz = plans[0]->esz;
+    std::unique_ptr<fm_batch> B(new fm_batch());
+    CUDA_TRY(cudaGetDevice(&B->device));
+    struct Item {
+      int level;
+      fmk::Step st;
+      int cls;
+      i64 tiles;
+    };
+    std::vector<Item> items;
+    std::vector<std::pair<int, size_t>> scratch_of;  // (op, bytes)
+    // scratch: one allocation for all operators
+    std::vector<size_t> op_off((size_t)num_ops + 1, 0);
+    const size_t align = 256;
+    for (int i = 0; i < num_ops; ++i) {
+      fm_plan *P = plans[i];
+      if (!P || P->ctype != ctype)
+        fail(FM_ERR_VALUE, "fm_batch_create: plans must share one compute "
+                           "type");
+      size_t bytes = 0;
+      if (num_cols[i] > 0)
+        for (i64 r : P->scratch_rows)
+          bytes += ((size_t)r * num_cols[i] * esz + align - 1) / align *
+                   align;
+      op_off[i + 1] = op_off[i] + bytes;
+    }
+    char *scratch = nullptr;
+    if (op_off[num_ops]) {
+      CUDA_TRY(cudaMalloc(&scratch, op_off[num_ops]));
+      B->allocs.push_back(scratch);
+    }
+    CUDA_TRY(cudaMalloc(&B->status, 2 * sizeof(int)));
+    B->allocs.push_back(B->status);
+    CUDA_TRY(cudaMemset(B->status, 0, 2 * sizeof(int)));
+    for (int i = 0; i < num_ops; ++i) {
+      fm_plan *P = plans[i];
+      const int dir = directions[i];
+      if (dir != FM_FORWARD && dir != FM_BACKWARD)
+        fail(FM_ERR_VALUE, "fm_batch_create: invalid direction");
+      const i64 M = num_cols[i];
+      if (M < 0) fail(FM_ERR_VALUE, "fm_batch_create: negative num_cols");
+      if (M == 0) continue;
+      const i64 n_in = dir == FM_FORWARD ? P->cols : P->rows;
+      const i64 n_out = dir == FM_FORWARD ? P->rows : P->cols;
+      if (!x[i] || !y[i] || (M > 1 && (ld_x[i] < n_in || ld_y[i] < n_out)))
+        fail(FM_ERR_VALUE, "fm_batch_create: bad operand of operator " +
+                               std::to_string(i));
+      if (!valid_type(x_types[i]) || !valid_type(y_types[i]))
+        fail(FM_ERR_TYPE, "fm_batch_create: unsupported element type");
+      std::vector<size_t> offs(P->scratch_rows.size());
+      size_t o = op_off[i];
+      for (size_t k = 0; k < P->scratch_rows.size(); ++k) {
+        offs[k] = o;
+        o += ((size_t)P->scratch_rows[k] * M * esz + align - 1) / align *
+             align;
+      }
+      int level = 0;
+      for (const LStep &ls0 : P->steps[dir]) {
+        LStep ls = ls0;
+        if (!configure(esz, ls, 0, 0, false))
+          fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "
+                                   "vector-major tile shape");
+        fmk::Step st = ls.st;
+        auto bind = [&](int id, const void *&ptr, int &type, i64 &ld) {
+          if (id == 0) {
+            ptr = x[i];
+            type = x_types[i];
+            ld = M > 1 ? ld_x[i] : n_in;
+          } else if (id == 1) {
+            ptr = y[i];
+            type = y_types[i];
+            ld = M > 1 ? ld_y[i] : n_out;
+          } else {
+            ptr = scratch + offs[id - 2];
+            type = P->io_type;
+            ld = P->scratch_rows[id - 2];
+          }
+        };
+        const void *sp, *dp;
+        bind(ls.src, sp, st.src_type, st.ld_src);
+        bind(ls.dst, dp, st.dst_type, st.ld_dst);
+        st.src = sp;
+        st.dst = const_cast<void *>(dp);
+        st.num_cols = M;
+        st.err = B->status + 1;
+        st.tma_in = st.tma_out = 0;
+        const i64 tiles = (st.V * M + st.B - 1) / st.B;
+        if (st.V * M >= 0x7fffffffLL)
+          fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
+        items.push_back(Item{level++, st, ls.cls, tiles});
+      }
+    }
+    if (items.empty()) fail(FM_ERR_VALUE, "fm_batch_create: no work");
+    std::stable_sort(items.begin(), items.end(),
+                     [](const Item &a, const Item &b) {
+                       return a.level < b.level;
+                     });
+    // one kernel class that covers every program of the batch
+    int cls = items[0].cls;
+    for (const Item &it : items) {
+      const int c = it.cls;
+      if (c == cls) continue;
+      if (c == 0 || cls == 0 || c == 3 || cls == 3) cls = 0;
+      else cls = 2;  // mixed power-of-two and odd-radix FFTs
+    }
+    if (ctype == FM_C128_DF) cls = 0;
+    std::vector<fmk::Step> steps;
+    std::vector<i64> start(1, 0);
+    std::vector<int> level(1, 0);
+    int max_B = 1;
+    size_t max_tile = 0;
+    i64 level_tiles = 0, max_level_tiles = 1;
+    for (size_t k = 0; k < items.size(); ++k) {
+      if (k > 0 && items[k].level != items[k - 1].level) {
+        level.push_back((int)k);
+        max_level_tiles = std::max(max_level_tiles, level_tiles);
+        level_tiles = 0;
+      }
+      steps.push_back(items[k].st);
+      start.push_back(start.back() + items[k].tiles);
+      level_tiles += items[k].tiles;
+      max_B = std::max(max_B, items[k].st.B);
+      max_tile = std::max(max_tile, fmk::tile_bytes(items[k].st.B,
+                                                   items[k].st.Lp, esz));
+    }
+    max_level_tiles = std::max(max_level_tiles, level_tiles);
+    level.push_back((int)items.size());
+    const size_t head =
+        ((sizeof(fmk::VInfo) + 12) * (size_t)max_B + 127) / 128 * 128;
+    const size_t smem = head + max_tile;
+    if (smem > (size_t)fmk::kMaxSmem)
+      fail(FM_ERR_UNSUPPORTED, "fm_batch_create: tile too large");
+    fmk::Step *dsteps = nullptr;
+    i64 *dstart = nullptr;
+    int *dlevel = nullptr;
+    CUDA_TRY(cudaMalloc(&dsteps, steps.size() * sizeof(fmk::Step)));
+    B->allocs.push_back(dsteps);
+    CUDA_TRY(cudaMalloc(&dstart, start.size() * sizeof(i64)));
+    B->allocs.push_back(dstart);
+    CUDA_TRY(cudaMalloc(&dlevel, level.size() * sizeof(int)));
+    B->allocs.push_back(dlevel);
+    CUDA_TRY(cudaMemcpy(dsteps, steps.data(),
+                        steps.size() * sizeof(fmk::Step),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dstart, start.data(), start.size() * sizeof(i64),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dlevel, level.data(), level.size() * sizeof(int),
+                        cudaMemcpyHostToDevice));
+    fmk::BatchLaunch &L = B->launch;
+    L.ctype = ctype;
+    L.cls = cls;
+    L.steps = dsteps;
+    L.start = dstart;
+    L.level = dlevel;
+    L.nlev = (int)level.size() - 1;
+    L.bar = reinterpret_cast<unsigned *>(B->status);
+    L.err = B->status + 1;
+    L.max_B = max_B;
+    L.smem = smem;
+    L.max_level_tiles = max_level_tiles;
+    B->num_steps = (i64)steps.size();
+    B->total_tiles = start.back();
+    *batch = B.release();
+    return FM_OK;
+  });
+}
+
+int fm_batch_execute(fm_batch *batch, void *stream) {
+  return guarded([&]() {
+    if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    const cudaStream_t s = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(batch->status, 0, sizeof(int), s));
+    CUDA_TRY(fmk::launch_batch(batch->launch, s));
+    return FM_OK;
+  });
+}
+
+int fm_batch_execute_graph(fm_batch *batch, void *stream) {
+  return guarded([&]() {
+    if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    if (!batch->exec) {
+      if (!batch->gstream)
+        CUDA_TRY(cudaStreamCreateWithFlags(&batch->gstream,
+                                           cudaStreamNonBlocking));
+      cudaGraph_t g = nullptr;
+      CUDA_TRY(cudaStreamBeginCapture(batch->gstream,
+                                      cudaStreamCaptureModeThreadLocal));
+      cudaError_t e1 =
+          cudaMemsetAsync(batch->status, 0, sizeof(int), batch->gstream);
+      cudaError_t e2 = e1 == cudaSuccess
+                           ? fmk::launch_batch(batch->launch, batch->gstream)
+                           : e1;
+      cudaError_t e3 = cudaStreamEndCapture(batch->gstream, &g);
+      CUDA_TRY(e2);
+      CUDA_TRY(e3);
+      cudaError_t e4 = cudaGraphInstantiate(&batch->exec, g, 0);
+      cudaGraphDestroy(g);
+      CUDA_TRY(e4);
+    }
+    CUDA_TRY(cudaGraphLaunch(batch->exec, (cudaStream_t)stream));
+    return FM_OK;
+  });
+}
+
+int fm_batch_check(fm_batch *batch) {
+  return guarded([&]() {
+    if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    CUDA_TRY(cudaDeviceSynchronize());
+    int v = 0;
+    CUDA_TRY(cudaMemcpy(&v, batch->status + 1, sizeof(int),
+                        cudaMemcpyDeviceToHost));
+    if (v) {
+      CUDA_TRY(cudaMemset(batch->status + 1, 0, sizeof(int)));
+      fail(v, "a bounded device wait of the batch gave up");
+    }
+    return FM_OK;
+  });
+}
+
+int fm_batch_get_info(const fm_batch *batch, int64_t *num_launches,
+                      int64_t *num_levels, int64_t *num_tiles) {
+  return guarded([&]() {
+    if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    if (num_launches) *num_launches = batch->num_steps;
+    if (num_levels) *num_levels = batch->launch.nlev;
+    if (num_tiles) *num_tiles = batch->total_tiles;
+    return FM_OK;
+  });
+}
+
+int fm_batch_destroy(fm_batch *batch) {
+  delete batch;
+  return FM_OK;
 }
 
 const char *fm_last_error(void) { return g_err.c_str(); }

@@ -1483,4 +1483,82 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
   if (!tma_in) cp_async_wait<0>();
 }
 
+
+// ------------------------------------------------------------ batches
+// Many operators in one persistent launch.  The launches of every operator's
+// plan are grouped into levels (level k holds the k-th launch of every plan);
+// level k + 1 reads what level k wrote, so the CTAs of the (cooperative)
+// launch meet at a grid barrier between levels.  Within a level the tiles of
+// all its steps form one index range, start[] holding each step's first
+// tile; every CTA walks it with stride gridDim.x.  Tiles are vector-major and
+// moved by plain loads and stores (one buffer), the step parameters are read
+// from global memory.
+
+// Bounded grid barrier: thread 0 of every CTA arrives on a counter and waits
+// until all gridDim.x CTAs of this phase have arrived.  Returns false (and
+// records FM_ERR_TIMEOUT) if the wait gives up; the caller then returns.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target,
+                                             int *err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    unsigned v = 0;
+    int it = 0;
+    for (;;) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];"
+                   : "=r"(v)
+                   : "l"(bar)
+                   : "memory");
+      if (v >= target || ++it > FM_WAIT_LIMIT) break;
+      __nanosleep(64);
+    }
+    ok = v >= target;
+    if (!ok && err) atomicExch(err, FM_ERR_TIMEOUT);
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <class E, int CLS>
+__global__ void __launch_bounds__(FM_MAX_THREADS, 1)
+    batch_kernel(const Step *__restrict__ steps, const i64 *__restrict__ start,
+                 const int *__restrict__ level, int nlev, unsigned *bar,
+                 int *err, int max_B) {
+  extern __shared__ __align__(128) unsigned char fm_smem[];
+  const int tid = threadIdx.x, T = blockDim.x;
+  VInfo *const vi = reinterpret_cast<VInfo *>(fm_smem);
+  i64 *sq = reinterpret_cast<i64 *>(vi + max_B);
+  int *sexp = reinterpret_cast<int *>(sq + max_B);
+  E *sm = reinterpret_cast<E *>(
+      fm_smem + ((sizeof(VInfo) * max_B + 8 * max_B + 4 * max_B + 127) &
+                 ~(size_t)127));
+  for (int l = 0; l < nlev; ++l) {
+    const int s0 = level[l], s1 = level[l + 1];
+    const i64 t1 = start[s1];
+    int k = s0;
+    for (i64 g = start[s0] + blockIdx.x; g < t1; g += gridDim.x) {
+      while (start[k + 1] <= g) ++k;
+      const Step &p = steps[k];
+      const i64 nvec = p.V * p.num_cols;
+      const FDiv dV((unsigned)p.V), dci((unsigned)p.vin.Cc),
+          dco((unsigned)p.vout.Cc);
+      setup_tile(p, vi, g - start[k], dV, dci, dco, nvec, tid, T);
+      if constexpr (Emu<E>::v)
+        for (int b = tid; b < p.B; b += T) sexp[b] = 0;
+      __syncthreads();
+      load_general<E, 0>(p, sm, vi, tid, T);
+      __syncthreads();
+      run_program<E, CLS, 0>(p, sm, p.Lp, p.B, vi, sq, tid, T);
+      store_tile<E, 0>(p, sm, vi, sexp, tid, T);
+      __syncthreads();
+    }
+    if (l + 1 < nlev &&
+        !grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err))
+      return;
+  }
+}
+
 }  // namespace fmk

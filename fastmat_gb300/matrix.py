@@ -395,6 +395,15 @@ class Matrix:
         return np.conj(self.backward(e))
 
 
+def _fcontig_tensor(t):
+    """2-D column-major view (n, M) of a tensor (copies if needed)."""
+    if t.dim() == 1:
+        t = t.unsqueeze(1)
+    if t.stride(0) == 1 and (t.shape[1] <= 1 or t.stride(1) >= t.shape[0]):
+        return t
+    return t.t().contiguous().t()
+
+
 def _is_tensor(x):
     t = type(x)
     return t.__module__.startswith('torch') and t.__name__ == 'Tensor'

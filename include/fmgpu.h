@@ -231,6 +231,37 @@ int fm_plan_get_info(const fm_plan *plan, fm_plan_info *info);
 int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
                      int64_t buf_len);
 
+/* ---- batches: many operators in one persistent launch -----------------
+ * A batch binds a list of plans (one operator each, forward or backward)
+ * to their operands: column-major x / y device buffers with num_cols
+ * columns each (leading dimensions ld_x / ld_y; types as in fm_execute).
+ * fm_batch_execute runs ALL of them in one cooperative persistent launch:
+ * the k-th launch of every plan forms level k, the tiles of a level are
+ * spread over all CTAs, and the CTAs meet at a grid barrier (a bounded
+ * wait) between levels.  Plans must share one compute type, FM_C64 or
+ * FM_C128_DF, and must outlive the batch (it reads their constants).  The
+ * batch owns the scratch every operator needs for its columns.
+ * fm_batch_execute_graph captures that launch into a CUDA graph on its
+ * first call (on a stream the batch owns) and replays the graph on `stream`
+ * from then on.  The operand pointers are fixed at creation, so a graph
+ * replay reads and writes the same buffers.  The reference applies its
+ * operators one call at a time; this has no counterpart there. */
+typedef struct fm_batch fm_batch;
+int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
+                    const int32_t *directions, const void *const *x,
+                    const int32_t *x_types, const int64_t *ld_x,
+                    void *const *y, const int32_t *y_types,
+                    const int64_t *ld_y, const int64_t *num_cols,
+                    fm_batch **batch);
+int fm_batch_execute(fm_batch *batch, void *stream);
+int fm_batch_execute_graph(fm_batch *batch, void *stream);
+/* Synchronises; FM_ERR_TIMEOUT if a bounded wait of the batch gave up. */
+int fm_batch_check(fm_batch *batch);
+/* Launches of the bound plans it replaces, levels, tiles. */
+int fm_batch_get_info(const fm_batch *batch, int64_t *num_launches,
+                      int64_t *num_levels, int64_t *num_tiles);
+int fm_batch_destroy(fm_batch *batch);
+
 /* ---- gradients of the differentiable path -----------------------------
  * Column reduction behind the parameter gradients of a chain of operators.
  * u, v (and w) are column-major arrays of num_cols columns whose columns are
