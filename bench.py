@@ -343,7 +343,7 @@ def run_gpu(args):
         xe.astype(dt32).T).cuda().t()).cpu().numpy()
     rel = float(np.max(np.abs(y32.astype(y64.dtype) - y64)) /
                 np.max(np.abs(y64)))
-    del y64, y32
+    del y32
 
     # e2e: host C ABI with pinned host buffers, copies inside the timed region
     e2e = None
@@ -414,6 +414,9 @@ def run_gpu(args):
     }
     if args.workload == 'chain':
         line["differentiable"] = measure_grad(torch, fg, args)
+    if args.workload == 'hadamard':
+        line["bf16_form"] = measure_bf16(torch, fg, args, build_fn, n_in, M,
+                                         xe, op64, peak, peak_kind)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload)
     if rank == 0:
@@ -421,6 +424,42 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def measure_bf16(torch, fg, args, build_fn, n_in, M, xe, op64, peak,
+                 peak_kind):
+    """The tensor-core form of the Hadamard workload: float32 data, the
+    16-point groups as BF16 MMA with FP32 accumulation (three-term split)."""
+    op, _, _ = build_fn(fg, 'bf16')
+    dt = np.float32
+    if not args.no_autotune:
+        op.autotune(M, out_dtype=np.float32)
+    xt = torch.from_numpy(xe.astype(dt).T).cuda().t()
+    ms, yt = time_device(torch, op, xt, args.steps, args.warmup,
+                         lambda: None)
+    y64 = op64.forward(torch.from_numpy(xe.T).cuda().t()).cpu().numpy()
+    rel = float(np.max(np.abs(yt.cpu().numpy().astype(np.float64) - y64)) /
+                np.max(np.abs(y64)))
+    plan = op.plan(np.float32)
+    code = fg._native.DTYPE_CODE
+    n_out = op.numRows
+    launches = np.mean(np.array([plan.execute_profiled(
+        fg._native.FORWARD, xt.data_ptr(), code[np.dtype(dt)], n_in,
+        yt.data_ptr(), code[np.dtype(dt)], n_out, M,
+        torch.cuda.current_stream().cuda_stream) for _ in range(3)]), axis=0)
+    nbytes = (n_in + n_out) * M * 4
+    k = int(np.argmax(launches))
+    ach = nbytes / (launches[k] * 1e-3) / 1e9
+    return {"value": nbytes / (ms * 1e-3) / 1e9, "unit": "GB/s",
+            "ms_per_step": ms, "dtype": "f32 data, bf16 x3 MMA, f32 accum",
+            "rel_err_vs_fp64": rel,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak,
+                         "traffic": ncu_traffic(args.workload, 'bf16', k + 1),
+                         "peak_kind": peak_kind,
+                         "kernel": "vprog launch %d of %d (tensor-core "
+                                   "FWHT groups)" % (k + 1, len(launches)),
+                         "launch_ms": [round(float(v), 4) for v in launches]}}
 
 
 def _time_events(torch, fn, steps, warmup):
@@ -788,9 +827,9 @@ def profile_target(args):
                           "operators": len(ops), "info": b.info()}))
         return
     build_fn, dt64, dt32, _ = WORKLOADS[args.workload]
-    prec = 'fp32' if args.form == 'fp32' else 'native'
+    prec = {'fp32': 'fp32', 'bf16': 'bf16'}.get(args.form, 'native')
     op, M, _ = build_fn(fg, prec)
-    dt = dt32 if args.form == 'fp32' else dt64
+    dt = dt64 if args.form == 'fp64' else dt32
     if not args.no_autotune:
         op.autotune(M, out_dtype=op._output_dtype(np.dtype(dt)))
     x = make_input(op.numCols, args.profile_target, dt, 5)
@@ -819,7 +858,8 @@ def main():
                     help='no timing: run the workload forward twice on COLS '
                          'columns with the tile shapes tuned for the full '
                          'column count (a small case for ncu captures)')
-    ap.add_argument('--form', default='fp64', choices=['fp64', 'fp32'],
+    ap.add_argument('--form', default='fp64',
+                    choices=['fp64', 'fp32', 'bf16'],
                     help='form run by --profile-target')
     args = ap.parse_args()
     if args.profile_target:

@@ -34,6 +34,7 @@ CODE_DTYPE = {v: k for k, v in DTYPE_CODE.items()}
 # compute types: float64 / complex128 in double-float arithmetic
 FM_F64_DF = 16
 FM_C128_DF = 17
+FM_F32_TC = 18   # float32, Hadamard 16-point groups on the tensor cores
 
 (NODE_FOURIER, NODE_CIRCULANT, NODE_TOEPLITZ, NODE_HADAMARD, NODE_DIAG,
  NODE_PARTIAL, NODE_PERMUTATION, NODE_PRODUCT, NODE_SUM, NODE_KRON,

@@ -36,6 +36,8 @@ cudaError_t launch_f32(const Step &st, int cls, int lay, int threads,
       if ((e = cfg(vprog_kernel<float, 0, 0>)) != cudaSuccess) return e;
       if ((e = cfg(vprog_kernel<float, 3, 0>)) != cudaSuccess) return e;
       if ((e = cfg(vprog_kernel<float, 3, 1>)) != cudaSuccess) return e;
+      if ((e = cfg(vprog_kernel<float, 4, 0>)) != cudaSuccess) return e;
+      if ((e = cfg(vprog_kernel<float, 4, 1>)) != cudaSuccess) return e;
       int dev = 0;
       if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
       if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
@@ -50,6 +52,8 @@ cudaError_t launch_f32(const Step &st, int cls, int lay, int threads,
       switch (key2) {
         case 6: e = occ(vprog_kernel<float, 3, 0>, threads, smem, &n); break;
         case 7: e = occ(vprog_kernel<float, 3, 1>, threads, smem, &n); break;
+        case 8: e = occ(vprog_kernel<float, 4, 0>, threads, smem, &n); break;
+        case 9: e = occ(vprog_kernel<float, 4, 1>, threads, smem, &n); break;
         default: e = occ(vprog_kernel<float, 0, 0>, threads, smem, &n); break;
       }
       if (e != cudaSuccess) return e;
@@ -66,6 +70,12 @@ cudaError_t launch_f32(const Step &st, int cls, int lay, int threads,
       break;
     case 7:
       vprog_kernel<float, 3, 1><<<(unsigned)g, threads, smem, s>>>(st);
+      break;
+    case 8:
+      vprog_kernel<float, 4, 0><<<(unsigned)g, threads, smem, s>>>(st);
+      break;
+    case 9:
+      vprog_kernel<float, 4, 1><<<(unsigned)g, threads, smem, s>>>(st);
       break;
     default:
       vprog_kernel<float, 0, 0><<<(unsigned)g, threads, smem, s>>>(st);

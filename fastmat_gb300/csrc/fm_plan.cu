@@ -56,6 +56,7 @@ int esize(int t) {
   switch (t) {
     case FM_F64_DF: return 8;
     case FM_C128_DF: return 16;
+    case FM_F32_TC: return 4;
     case FM_I8: return 1;
     case FM_I16: return 2;
     case FM_I32: return 4;
@@ -72,7 +73,10 @@ bool is_cplx(int t) {
 }
 // element type of the buffers a plan of compute type t reads and writes
 int io_of(int t) {
-  return t == FM_F64_DF ? FM_F64 : t == FM_C128_DF ? FM_C128 : t;
+  return t == FM_F64_DF    ? FM_F64
+         : t == FM_C128_DF ? FM_C128
+         : t == FM_F32_TC  ? FM_F32
+                           : t;
 }
 bool valid_type(int t) { return t >= FM_I8 && t <= FM_C128; }
 
@@ -317,15 +321,22 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   fmk::Step &st = ls.st;
   const int L = std::max(st.L, 1);
   const int ept = ls.ept;
+  // the tensor-core FWHT (class 4) works on whole warpgroups and needs
+  // its staging area and TMEM bookkeeping beyond the tile ring
+  const int tgran = ls.cls == 4 ? 128 : 32;
+  const size_t extra = ls.cls == 4 ? (size_t)fmk::kTcBytes + 1024 : 0;
   auto threads_for = [&](int b) {
     i64 t = ((i64)b * L + ept - 1) / ept;
-    t = (t + 31) / 32 * 32;
-    return (int)std::max<i64>(t, 32);
+    t = (t + tgran - 1) / tgran * tgran;
+    return (int)std::max<i64>(t, tgran);
+  };
+  auto lsmem = [&](int B, int Lp, int nb) {
+    return fmk::launch_smem(B, Lp, esz, nb) + extra;
   };
   auto pick_nbuf = [&](int B, int Lp) {
     if (want_nbuf) return want_nbuf;
     int nb = 4;
-    while (nb > 2 && fmk::launch_smem(B, Lp, esz, nb) > (size_t)150 * 1024)
+    while (nb > 2 && lsmem(B, Lp, nb) > (size_t)150 * 1024)
       --nb;
     return nb;
   };
@@ -335,7 +346,8 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   // element-major tiles: strided input and output views whose inner extent
   // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
   // budget allows, never below 16 B), moved by TMA boxes
-  if (allow_em && (ls.cls == 1 || ls.cls == 3) && st.vin.Cc > 1 &&
+  if (allow_em && (ls.cls == 1 || ls.cls == 3 || ls.cls == 4) &&
+      st.vin.Cc > 1 &&
       st.vout.Cc > 1) {
     int B = want_B ? want_B : 128 / esz;
     if (!want_B) {
@@ -345,7 +357,7 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
     if (B * esz >= 16 && threads_for(B) <= FM_MAX_THREADS &&
         st.V % B == 0 && st.vin.Cc % B == 0 && st.vout.Cc % B == 0) {
       const int nbuf = pick_nbuf(B, L);
-      const size_t smem = fmk::launch_smem(B, L, esz, nbuf);
+      const size_t smem = lsmem(B, L, nbuf);
       if (smem <= (size_t)fmk::kMaxSmem) {
         ls.lay = 1;
         st.B = B;
@@ -377,7 +389,7 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   if (((Lp / gran) & 1) == 0) Lp += gran;
   const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
   auto smem_for = [&](int b, int nb) {
-    return fmk::launch_smem(b, Lp, esz, nb);
+    return lsmem(b, Lp, nb);
   };
   int B;
   if (want_B) {
@@ -485,7 +497,8 @@ class Planner {
           ((float *)buf.data())[4 * i + 2] = hi(v[i].imag());
           ((float *)buf.data())[4 * i + 3] = lo(v[i].imag());
           break;
-        case FM_F32: ((float *)buf.data())[i] = (float)v[i].real(); break;
+        case FM_F32:
+        case FM_F32_TC: ((float *)buf.data())[i] = (float)v[i].real(); break;
         case FM_F64: ((double *)buf.data())[i] = v[i].real(); break;
         case FM_I64:
           ((int64_t *)buf.data())[i] = (int64_t)llround(v[i].real());
@@ -762,6 +775,7 @@ class Planner {
 
   fmk::Op fwht_op(i64 n) {
     fmk::Op o = mkop(fmk::OP_FWHT, (int)n);
+    o.sign = P_->ctype == FM_F32_TC ? 1 : 0;  // 16-point groups on MMA
     int bits = 0;
     while ((1LL << bits) < n) ++bits;
     const int g = 4;
@@ -1247,7 +1261,7 @@ class Planner {
       if (o.kind == fmk::OP_GATHER || o.kind == fmk::OP_DENSE) gen = true;
     }
     if (gen || (fft && fwht)) return 0;
-    if (fwht) return 3;
+    if (fwht) return P_->ctype == FM_F32_TC ? 4 : 3;
     if (fft) return odd ? 2 : 1;
     return 3;
   }
@@ -1688,7 +1702,8 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
     fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
   cudaError_t e;
   switch (P->ctype) {
-    case FM_F32: e = fmk::launch_f32(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
+    case FM_F32:
+    case FM_F32_TC: e = fmk::launch_f32(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     case FM_F64: e = fmk::launch_f64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     case FM_C64: e = fmk::launch_c64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
     case FM_I64: e = fmk::launch_i64(st, ls.cls, ls.lay, ls.threads, ls.smem, grid, s); break;
@@ -1883,7 +1898,7 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
     if (compute_type != FM_F32 && compute_type != FM_F64 &&
         compute_type != FM_C64 && compute_type != FM_C128 &&
         compute_type != FM_I64 && compute_type != FM_F64_DF &&
-        compute_type != FM_C128_DF)
+        compute_type != FM_C128_DF && compute_type != FM_F32_TC)
       fail(FM_ERR_TYPE, "unsupported compute type");
     std::vector<NodeRec> recs((size_t)num_nodes);
     for (int i = 0; i < num_nodes; ++i) {

@@ -15,6 +15,8 @@
 
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "fm_types.cuh"
 
 namespace fmk {
@@ -389,6 +391,10 @@ __device__ __forceinline__ E *vbase(E *sm, int b, int Lp) {
   else return sm + b * Lp;
 }
 
+}  // namespace fmk
+#include "fm_tc.cuh"
+namespace fmk {
+
 // ------------------------------------------------------------ FFT stages
 // In-place mixed-radix stages.  With L = R_1 ... R_S and M_0 = L,
 // M_s = M_{s-1} / R_s, stage s of the DIF transform takes, for every block
@@ -578,10 +584,19 @@ __device__ __forceinline__ void fwht_pass(E *sm, int Lp, int B, int Lf, int s,
 }
 
 template <class E, int LAY>
-__device__ void run_fwht(const Op &op, E *sm, int Lp, int B, int tid, int T) {
+__device__ void run_fwht(const Op &op, E *sm, int Lp, int B, int tid, int T,
+                         TcState *tc = nullptr) {
   int s = 0;
   for (int p = 0; p < op.nrad; ++p) {
     const int K = op.rad[p];
+    if constexpr (std::is_same<E, float>::value) {
+      // 16-point groups on the tensor cores (op.sign marks the form)
+      if (tc && op.sign && K == 4 && !tc->failed) {
+        run_h16tc<LAY>(sm, Lp, B, op.len, s, *tc, tid, T);
+        s += K;
+        continue;
+      }
+    }
     switch (K) {
       case 1: fwht_pass<1, LAY>(sm, Lp, B, op.len, s, tid, T); break;
       case 2: fwht_pass<2, LAY>(sm, Lp, B, op.len, s, tid, T); break;
@@ -1280,7 +1295,8 @@ __device__ __forceinline__ void emu_out_em(const Step &p, E *sm,
 template <class E, int CLS, int LAY>
 __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
                                             int B, const VInfo *vi, i64 *sq,
-                                            int tid, int T) {
+                                            int tid, int T,
+                                            TcState *tc = nullptr) {
   for (int o = 0; o < p.nops; ++o) {
     const Op &op = p.ops[o];
     switch (op.kind) {
@@ -1290,8 +1306,8 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
           run_fft<E, CLS, LAY>(op, sm, Lp, B, tid, T);
         break;
       case OP_FWHT:
-        if constexpr (CLS == 0 || CLS == 3)
-          run_fwht<E, LAY>(op, sm, Lp, B, tid, T);
+        if constexpr (CLS == 0 || CLS == 3 || CLS == 4)
+          run_fwht<E, LAY>(op, sm, Lp, B, tid, T, tc);
         break;
       case OP_GATHER:
         if constexpr (CLS == 0 && LAY == 0)
@@ -1316,7 +1332,8 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // CLS selects the op subset compiled into an instantiation, so the hot
 // programs (power-of-two FFT, FWHT) do not carry the register pressure of
 // the rarely used ops: 1 = pow2 FFT + pointwise, 2 = FFT with radices 3/5/7,
-// 3 = FWHT + pointwise, 0 = everything.  LAY is the tile layout.
+// 3 = FWHT + pointwise, 4 = FWHT with 16-point groups on the tensor cores
+// (float only) + pointwise, 0 = everything.  LAY is the tile layout.
 //
 // Persistent CTAs: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x,
 // ...  Tiles are copied into a ring of p.nbuf shared-memory buffers
@@ -1358,6 +1375,14 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
       mbar_init_fence();
     }
     __syncthreads();
+  }
+  TcState tcs;
+  TcState *tc = nullptr;
+  if constexpr (CLS == 4) {
+    const size_t off =
+        (launch_smem(B, Lp, sizeof(E), NB) + 1023) & ~(size_t)1023;
+    tc_init(tcs, fm_smem + off, p.err, tid);
+    tc = &tcs;
   }
 
   i64 tile = blockIdx.x;
@@ -1427,7 +1452,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
       __syncthreads();
     }
 
-    run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T);
+    run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc);
 
     if (tma_out) {
       if constexpr (LAY == 1) {
@@ -1481,6 +1506,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, 1)
   }
   if (tma_out) bulk_wait_all();
   if (!tma_in) cp_async_wait<0>();
+  if constexpr (CLS == 4) tc_release(tcs, tid);
 }
 
 

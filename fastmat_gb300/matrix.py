@@ -102,6 +102,8 @@ def _compute_code(out_dtype, precision='native'):
     dt = np.dtype(out_dtype)
     if dt.kind in 'iub':
         return _native.FM_I64
+    if precision == 'bf16' and dt == np.float32:
+        return _native.FM_F32_TC
     if precision != 'fp64':
         if dt == np.complex128:
             return _native.FM_C128_DF
@@ -120,7 +122,10 @@ class Matrix:
     is done: ``'native'`` (default: float64 / complex128 results computed in
     double-float arithmetic on the FP32 pipes), ``'fp64'`` (the FP64 pipe)
     or ``'fp32'`` (opt-in reduced precision: float32 / complex64 arithmetic
-    and output).
+    and output) or ``'bf16'`` (as 'fp32', and the 16-point groups of
+    Hadamard transforms on float32 data run on the tensor cores as BF16
+    matrix products with FP32 accumulation, the operand split exactly into
+    three BF16 terms).
     """
 
     _array = None
@@ -141,8 +146,9 @@ class Matrix:
         self._minType = T.supported(options.get('minType', np.int8))
         self._widenInputDatatype = options.get('widenInputDatatype', False)
         prec = options.get('precision', 'native')
-        if prec not in ('native', 'fp32', 'fp64'):
-            raise ValueError("precision must be 'native', 'fp64' or 'fp32'")
+        if prec not in ('native', 'fp32', 'fp64', 'bf16'):
+            raise ValueError(
+                "precision must be 'native', 'fp64', 'fp32' or 'bf16'")
         self._precision = prec
         self._plans = {}
 
@@ -258,7 +264,7 @@ class Matrix:
     def _output_dtype(self, x_dtype):
         internal = T.promote(x_dtype, self._minType)
         out = T.promote(internal, self._dtype)
-        if self._precision == 'fp32':
+        if self._precision in ('fp32', 'bf16'):
             out = T.single(out)
         return out
 

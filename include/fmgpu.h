@@ -106,6 +106,12 @@ typedef struct fm_node {
  * runs far faster than its FP64 pipe; buffers keep float64 / complex128 */
 #define FM_F64_DF 16
 #define FM_C128_DF 17
+/* float32 data whose Hadamard transforms run their 16-point groups on the
+ * tensor cores: each group is a 16 x 16 +-1 matrix product in BF16 with
+ * FP32 accumulation, the float32 operand split exactly into three BF16
+ * terms (relative error of the order of float32's); everything else in
+ * float32.  Buffers are float32. */
+#define FM_F32_TC 18
 
 /* plan precisions */
 #define FM_PREC_NATIVE 0  /* compute in the operator/input promoted type     */

@@ -217,3 +217,37 @@ def test_pointwise_folded_into_long_transforms(expr, rin):
     g = cplx(rng, op.numRows, 3)
     assert fo.rel_err(op.forward(x), oop.forward(x)) <= 1e-12
     assert fo.rel_err(op.backward(g), oop.backward(g)) <= 1e-12
+
+
+@pytest.mark.parametrize('order,cols', [(4, 3), (8, 5), (12, 2), (13, 3),
+                                        (17, 2), (22, 2)])
+def test_hadamard_tensor_core_form(order, cols):
+    """precision='bf16': 16-point groups as BF16 MMA (three-term split,
+    FP32 accumulation) on the tensor cores; error against FP64 stated and
+    bounded by 1e-5."""
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(order)
+    x = rng.standard_normal((1 << order, cols)).astype(np.float32)
+    H = fg.Hadamard(order, precision='bf16')
+    y = H.forward(x)
+    assert y.dtype == np.float32
+    ref = fo.Hadamard(order).forward(x.astype(np.float64))
+    err = fo.rel_err(y, ref)
+    assert err <= 1e-5, err
+    desc = H.plan(np.float32).describe()
+    assert 'cls=4' in desc
+    z = H.backward(x)
+    assert fo.rel_err(z, ref) <= 1e-5
+
+
+def test_kron_with_tensor_core_hadamard_mode():
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(3)
+    d = rng.standard_normal(16)
+    op = fg.Kron(fg.Hadamard(4), fg.Diag(d), fg.Hadamard(8),
+                 precision='bf16')
+    oop = fo.Kron(fo.Hadamard(4), fo.Diag(d), fo.Hadamard(8))
+    x = rng.standard_normal((op.numCols, 3)).astype(np.float32)
+    y = op.forward(x)
+    assert y.dtype == np.float32
+    assert fo.rel_err(y, oop.forward(x.astype(np.float64))) <= 1e-5
