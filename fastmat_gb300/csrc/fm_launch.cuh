@@ -39,6 +39,17 @@ struct BatchLaunch {
 };
 cudaError_t launch_batch(const BatchLaunch &b, cudaStream_t s);
 
+// largest FFT radix the kernels of a compute type are built with (see
+// MinBlocks / Radix16 in fm_vprog.cuh): 8 for single precision and
+// double-float, 16 otherwise
+inline int max_radix_for(int ctype) {
+  return (ctype == 4 /* FM_F32 */ || ctype == 6 /* FM_C64 */ ||
+          ctype == 16 /* FM_F64_DF */ || ctype == 17 /* FM_C128_DF */ ||
+          ctype == 18 /* FM_F32_TC */)
+             ? 8
+             : 16;
+}
+
 // records the message fm_last_error() returns on the calling thread
 void set_last_error(const char *msg);
 

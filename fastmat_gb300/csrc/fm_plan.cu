@@ -746,8 +746,8 @@ class Planner {
         r.push_back(p);
         n /= p;
       }
-    // largest radix: 16, except 8 for double-float (register budget)
-    const int big = P_->ctype == FM_C128_DF ? 8 : 16;
+    // largest radix the kernels of this compute type are built with
+    const int big = fmk::max_radix_for(P_->ctype);
     while (n % big == 0) {
       r.push_back(big);
       n /= big;

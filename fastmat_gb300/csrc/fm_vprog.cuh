@@ -474,6 +474,24 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
   __syncthreads();
 }
 
+// Register budget per element type: the single-precision kernels run two
+// 512-thread CTAs per SM (64 registers per thread) to hide more latency,
+// which leaves no room for radix-16 butterflies; the wider types keep one
+// CTA per SM and radix 16 (double-float tops out at radix 8).  The planner
+// picks radices with the same rule (max_radix_for in fm_launch.cuh).
+template <class E, int CLS> struct MinBlocks {
+  static constexpr int v = ((std::is_same<E, float>::value ||
+                             std::is_same<E, float2>::value) &&
+                            CLS != 4)
+                               ? 2
+                               : 1;
+};
+template <class C> struct Radix16 {
+  static constexpr bool v =
+      !Emu<C>::v && !std::is_same<C, float2>::value &&
+      !std::is_same<C, float>::value;
+};
+
 template <bool DIT, int CLS, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage_s(int R, C *sm, int Lp, int B,
                                             int Lf, int Mprev, const C *tw,
@@ -484,7 +502,7 @@ __device__ __forceinline__ void fft_stage_s(int R, C *sm, int Lp, int B,
     case 8: fft_stage<8, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
     case 16:
       // double-float vectors of 16 elements do not fit the register budget
-      if constexpr (!Emu<C>::v)
+      if constexpr (Radix16<C>::v)
         fft_stage<16, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
       break;
     case 3:
@@ -1345,7 +1363,7 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // nbuf tile buffers, nbuf mbarriers, nbuf sets of VInfo records, per-vector
 // scalars.
 template <class E, int CLS, int LAY>
-__global__ void __launch_bounds__(FM_MAX_THREADS, 1)
+__global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
     vprog_kernel(const __grid_constant__ Step p) {
   extern __shared__ __align__(128) unsigned char fm_smem[];
   const int tid = threadIdx.x, T = blockDim.x;
@@ -1549,7 +1567,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target,
 }
 
 template <class E, int CLS>
-__global__ void __launch_bounds__(FM_MAX_THREADS, 1)
+__global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
     batch_kernel(const Step *__restrict__ steps, const i64 *__restrict__ start,
                  const int *__restrict__ level, int nlev, unsigned *bar,
                  int *err, int max_B) {
