@@ -407,6 +407,16 @@ namespace fmk {
 // natural order; with opposite signs the two are inverse up to the factor L.
 // Each work item reads and writes the same R positions, so a stage needs one
 // barrier and holds only R values per thread.
+// Barrier of the threads that run one tile program together: the whole CTA,
+// or a single warp when the tile's vectors are divided among warps (T == 32;
+// a 32-thread CTA is one warp too).
+__device__ __forceinline__ void group_sync(int T) {
+  if (T <= 32)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
 template <int R, bool DIT, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
                                           int Mprev,
@@ -471,7 +481,7 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
       }
     }
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 // Register budget per element type: the single-precision kernels run two
@@ -598,7 +608,7 @@ __device__ __forceinline__ void fwht_pass(E *sm, int Lp, int B, int Lf, int s,
       for (int r = 0; r < R; ++r) vec[jx<E, LAY>(base + (r << s), B)] = v[r];
     }
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 template <class E, int LAY>
@@ -644,14 +654,14 @@ __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
       }
     }
   }
-  __syncthreads();
+  group_sync(T);
   {
     Walk w(tid, op.len, T);
 #pragma unroll
     for (int i = 0; i < MB; ++i, w.next())
       if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 template <class E>
@@ -676,14 +686,14 @@ __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
       }
     }
   }
-  __syncthreads();
+  group_sync(T);
   {
     Walk w(tid, rows, T);
 #pragma unroll
     for (int i = 0; i < MB; ++i, w.next())
       if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 template <class E, int LAY>
@@ -692,7 +702,7 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
   const bool per_vec = op.kind == OP_MUL || op.kind == OP_TW;
   if (per_vec) {
     for (int b = tid; b < B; b += T) sq[b] = (vi[b].vcol / op.div) % op.mod;
-    __syncthreads();
+    group_sync(T);
   }
   const int len = op.len;
   const int total = B * len;
@@ -719,7 +729,10 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
       case OP_TW: {
         if constexpr (Tr<E>::cplx) {
           const int nat = op.ptr2 ? op.ptr2[j] : j;
-          const i64 t = (sq[b] * (i64)nat) % op.N;
+          // q * nat < N in the four-step passes (q < N / len, nat < len):
+          // reduce only when a product reaches N
+          i64 t = sq[b] * (i64)nat;
+          if (t >= op.N) t %= op.N;
           const E wv = ((const E *)op.ptr)[t];
           *e = op.sign < 0 ? cmul(*e, wv) : cmulc(*e, wv);
         }
@@ -728,7 +741,7 @@ __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
       default: break;
     }
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 template <class E, int LAY>
@@ -748,7 +761,7 @@ __device__ void run_zpad(const Op &op, E *sm, int Lp, int B, int tid, int T) {
     }
     vbase<E, LAY>(sm, b, Lp)[jx<E, LAY>(op.len + j, B)] = zero<E>();
   }
-  __syncthreads();
+  group_sync(T);
 }
 
 // ------------------------------------------------------------ async copies
@@ -1362,6 +1375,16 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // results leave by TMA box stores.  Dynamic shared memory (launch_smem):
 // nbuf tile buffers, nbuf mbarriers, nbuf sets of VInfo records, per-vector
 // scalars.
+// Whether the warps of a CTA can run the tile program on disjoint sets of
+// vectors (vector-major tiles whose B vectors divide evenly among the warps,
+// few enough elements per warp for the register-staged ops), so that the
+// program's stages need warp barriers only.
+template <class E, int CLS, int LAY>
+__device__ __forceinline__ bool warp_mode(int B, int L, int nwarps) {
+  return LAY == 0 && CLS != 4 && nwarps > 1 && B % nwarps == 0 &&
+         (B / nwarps) * L <= 32 * Ept<E>::v;
+}
+
 template <class E, int CLS, int LAY>
 __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
     vprog_kernel(const __grid_constant__ Step p) {
@@ -1386,6 +1409,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
   const bool async_in = tma_in || (p.src_type == Tr<E>::code && !p.map_in);
   const bool fixup = p.conj_in || p.pre;
   const i64 G = gridDim.x;
+  const int nwarps = T >> 5;
+  const bool wmode = warp_mode<E, CLS, LAY>(B, p.L, nwarps);
 
   if (tma_in) {
     if (tid == 0) {
@@ -1470,7 +1495,15 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       __syncthreads();
     }
 
-    run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc);
+    if (wmode) {
+      // each warp runs the program on its own B / nwarps vectors
+      const int w = tid >> 5, vw = B / nwarps;
+      run_program<E, CLS, LAY>(p, sm + w * vw * Lp, Lp, vw, vi + w * vw,
+                               sq + w * vw, tid & 31, 32, tc);
+      __syncthreads();
+    } else {
+      run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc);
+    }
 
     if (tma_out) {
       if constexpr (LAY == 1) {
@@ -1595,7 +1628,15 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       __syncthreads();
       load_general<E, 0>(p, sm, vi, tid, T);
       __syncthreads();
-      run_program<E, CLS, 0>(p, sm, p.Lp, p.B, vi, sq, tid, T);
+      const int nwarps = T >> 5;
+      if (warp_mode<E, CLS, 0>(p.B, p.L, nwarps)) {
+        const int w = tid >> 5, vw = p.B / nwarps;
+        run_program<E, CLS, 0>(p, sm + w * vw * p.Lp, p.Lp, vw, vi + w * vw,
+                               sq + w * vw, tid & 31, 32);
+        __syncthreads();
+      } else {
+        run_program<E, CLS, 0>(p, sm, p.Lp, p.B, vi, sq, tid, T);
+      }
       store_tile<E, 0>(p, sm, vi, sexp, tid, T);
       __syncthreads();
     }
