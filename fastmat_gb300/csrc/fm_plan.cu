@@ -415,10 +415,14 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   ls.threads = threads_for(B);
   ls.smem = smem;
   // contiguous vectors move by 1-D bulk copies of their 128-byte chunks
-  ls.tma_in_ok = st.vin.Cc == 1 && st.in_len == L && st.in_len == st.vin.n &&
+#ifndef FM_VM_BULK
+#define FM_VM_BULK 1
+#endif
+  ls.tma_in_ok = FM_VM_BULK && st.vin.Cc == 1 && st.in_len == L && st.in_len == st.vin.n &&
                  !st.map_in && st.in_rows == st.vin.A * st.vin.n &&
                  ((i64)st.in_len * esz) % 16 == 0;
-  ls.tma_out_ok = st.vout.Cc == 1 && st.out_len == st.vout.n &&
+  ls.tma_out_ok = FM_VM_BULK && st.vout.Cc == 1 &&
+                  st.out_len == st.vout.n &&
                   st.out_mode == 0 && !st.accumulate &&
                   st.out_rows == st.vout.A * st.vout.n &&
                   ((i64)st.out_len * esz) % 16 == 0;

@@ -811,11 +811,13 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
       "r"(bytes)
       : "memory");
 }
+// one poll; the thread may be suspended inside it for up to ~1 us while the
+// phase is incomplete (it resumes as soon as the phase completes)
 __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
   unsigned done;
   asm volatile(
       "{\n .reg .pred p;\n"
-      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000;\n"
       " selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(done)
       : "r"(bar), "r"(phase)
@@ -1468,9 +1470,13 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
         cp_async_commit();
         cp_async_wait_n(NB - 1);
       } else {
-        const bool ok = mbar_wait(smem_addr(bars + cur),
-                                  (phase_bits >> cur) & 1u, FM_WAIT_LIMIT);
-        // block-wide vote so that every thread leaves the loop together
+        // one warp polls the barrier, the others wait at the block barrier
+        // (which issues no instructions); the vote then tells every thread
+        // whether the copy landed, so all leave the loop together
+        bool ok = true;
+        if (tid < 32)
+          ok = mbar_wait(smem_addr(bars + cur), (phase_bits >> cur) & 1u,
+                         FM_WAIT_LIMIT);
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
