@@ -90,3 +90,14 @@ cudaError_t launch_c64(const Step &st, int cls, int lay, int threads,
 }
 
 }  // namespace fmk
+
+#if FM_PHASE_TIMING
+extern "C" int fm_debug_phase_cycles(unsigned long long *out, int reset) {
+  if (cudaMemcpyFromSymbol(out, fmk::g_phase_cycles, 8 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  if (reset) {
+    unsigned long long z[8] = {0};
+    cudaMemcpyToSymbol(fmk::g_phase_cycles, z, sizeof(z));
+  }
+  return 0;
+}
+#endif

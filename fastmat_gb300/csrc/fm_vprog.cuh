@@ -696,50 +696,83 @@ __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
   group_sync(T);
 }
 
+// one pass over the B x len elements of a tile applying f(element, b, j)
+template <class E, int LAY, class F>
+__device__ __forceinline__ void ew_loop(E *sm, int Lp, int B, int len,
+                                        int tid, int T, F f) {
+  const int total = B * len;
+  if constexpr (LAY == 1) {
+    const int lgB = __ffs(B) - 1;
+    for (int g = tid; g < total; g += T) {
+      const int b = g & (B - 1), j = g >> lgB;
+      f(sm[j * B + b], b, j);
+    }
+  } else {
+    Walk w(tid, len, T);
+    for (int g = tid; g < total; g += T, w.next())
+      f(sm[w.b * Lp + pidx<E>(w.j)], w.b, w.j);
+  }
+}
+
 template <class E, int LAY>
 __device__ void run_elementwise(const Op &op, E *sm, int Lp, int B,
                                 const VInfo *vi, i64 *sq, int tid, int T) {
-  const bool per_vec = op.kind == OP_MUL || op.kind == OP_TW;
-  if (per_vec) {
-    for (int b = tid; b < B; b += T) sq[b] = (vi[b].vcol / op.div) % op.mod;
+  const int kind = op.kind;
+  if (kind == OP_MUL || kind == OP_TW) {
+    // vcol < 2^31: 32-bit arithmetic, nothing to do for the common
+    // div = mod = 1 (sq = 0)
+    if (op.div == 1 && op.mod == 1) {
+      for (int b = tid; b < B; b += T) sq[b] = 0;
+    } else {
+      for (int b = tid; b < B; b += T)
+        sq[b] = ((unsigned)vi[b].vcol / (unsigned)op.div) % (unsigned)op.mod;
+    }
     group_sync(T);
   }
   const int len = op.len;
-  const int total = B * len;
-  const int lgB = __ffs(B) - 1;
-  Walk w(tid, len, T);
-  for (int f = tid; f < total; f += T, w.next()) {
-    int b, j;
-    if constexpr (LAY == 1) {
-      b = f & (B - 1);
-      j = f >> lgB;
-    } else {
-      b = w.b;
-      j = w.j;
+  switch (kind) {
+    case OP_MUL: {
+      // the table holds mod * stride < 2^31 entries: 32-bit indices
+      const E *P = (const E *)op.ptr;
+      const int stride = op.stride;
+      if (op.sign)
+        ew_loop<E, LAY>(sm, Lp, B, len, tid, T, [&](E &e, int b, int j) {
+          e = mulv(e, P[(int)sq[b] * stride + j], true);
+        });
+      else
+        ew_loop<E, LAY>(sm, Lp, B, len, tid, T, [&](E &e, int b, int j) {
+          e = mulv(e, P[(int)sq[b] * stride + j], false);
+        });
+      break;
     }
-    E *e = vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B);
-    switch (op.kind) {
-      case OP_MUL: {
-        const E m = ((const E *)op.ptr)[sq[b] * op.stride + j];
-        *e = mulv(*e, m, op.sign != 0);
-        break;
-      }
-      case OP_SCALE: *e = mulv(*e, scalar_of<E>(op.sre, op.sim), false); break;
-      case OP_CONJ: *e = conjv(*e); break;
-      case OP_TW: {
-        if constexpr (Tr<E>::cplx) {
-          const int nat = op.ptr2 ? op.ptr2[j] : j;
-          // q * nat < N in the four-step passes (q < N / len, nat < len):
-          // reduce only when a product reaches N
+    case OP_SCALE: {
+      const E c = scalar_of<E>(op.sre, op.sim);
+      ew_loop<E, LAY>(sm, Lp, B, len, tid, T,
+                      [&](E &e, int, int) { e = mulv(e, c, false); });
+      break;
+    }
+    case OP_CONJ:
+      ew_loop<E, LAY>(sm, Lp, B, len, tid, T,
+                      [&](E &e, int, int) { e = conjv(e); });
+      break;
+    case OP_TW:
+      if constexpr (Tr<E>::cplx) {
+        const E *tw = (const E *)op.ptr;
+        const int *perm = op.ptr2;
+        const i64 N = op.N;
+        const bool neg = op.sign < 0;
+        ew_loop<E, LAY>(sm, Lp, B, len, tid, T, [&](E &e, int b, int j) {
+          const int nat = perm ? perm[j] : j;
+          // q * nat < N in the four-step passes (q < N / len,
+          // nat < len): reduce only when a product reaches N
           i64 t = sq[b] * (i64)nat;
-          if (t >= op.N) t %= op.N;
-          const E wv = ((const E *)op.ptr)[t];
-          *e = op.sign < 0 ? cmul(*e, wv) : cmulc(*e, wv);
-        }
-        break;
+          if (t >= N) t %= N;
+          const E wv = tw[t];
+          e = neg ? cmul(e, wv) : cmulc(e, wv);
+        });
       }
-      default: break;
-    }
+      break;
+    default: break;
   }
   group_sync(T);
 }
@@ -1045,15 +1078,18 @@ __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
   }
   const bool any = p.post || p.has_scale || p.conj_out || Emu<E>::v;
   if (!any) return;
+  const E *post = (const E *)p.post;
+  const bool has_scale = p.has_scale != 0, cj = p.conj_out != 0;
+  const E c = scalar_of<E>(p.scale_re, p.scale_im);
   Walk w(tid, n, T);
   for (int f = tid; f < total; f += T, w.next()) {
     const int b = w.b, j = w.j;
     E *e = sm + b * Lp + pidx<E>(j);
     E val = *e;
-    if (p.post && vi[b].rb_out >= 0)
-      val = mulv(val, ((const E *)p.post)[vi[b].rb_out + j], false);
-    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
-    if (p.conj_out) val = conjv(val);
+    if (post && vi[b].rb_out >= 0)
+      val = mulv(val, post[vi[b].rb_out + j], false);
+    if (has_scale) val = mulv(val, c, false);
+    if (cj) val = conjv(val);
     if constexpr (Emu<E>::v) val = to_bits(val, sexp[b]);
     *e = val;
   }
@@ -1188,6 +1224,7 @@ __device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
     __syncthreads();
   }
   if (!p.post && !p.has_scale && !p.conj_out) return;
+  const E c = scalar_of<E>(p.scale_re, p.scale_im);
   for (int f = tid; f < total; f += T) {
     const int b = f & (B - 1), j = f >> lgB;
     E val = sm[f];
@@ -1195,7 +1232,7 @@ __device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
       const i64 rb = vi[b].rb_out;
       if (rb >= 0) val = mulv(val, ((const E *)p.post)[rb + (i64)j * cc], false);
     }
-    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
+    if (p.has_scale) val = mulv(val, c, false);
     if (p.conj_out) val = conjv(val);
     sm[f] = val;
   }
@@ -1208,6 +1245,7 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
                                            int tid, int T) {
   const int B = p.B, Lp = p.Lp;
   const bool acc = p.accumulate != 0;
+  const E c = scalar_of<E>(p.scale_re, p.scale_im);
   if constexpr (LAY == 0) {
     if (p.out_mode == 1) {
       // gather: out row i of column m takes vector element map_out[i]
@@ -1218,7 +1256,7 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
         const i64 j = p.map_out[i];
         E val = j < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)j)];
         if (j >= 0 && p.post) val = mulv(val, ((const E *)p.post)[j], false);
-        if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
+        if (p.has_scale) val = mulv(val, c, false);
         if (p.conj_out) val = conjv(val);
         store_as<E>(p.dst, p.dst_type, vi[b].col_dst + i, val, acc,
                     Emu<E>::v ? sexp[b] : 0);
@@ -1248,7 +1286,7 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
     E val = vbase<E, LAY>(const_cast<E *>(sm), b, Lp)
         [jx<E, LAY>(p.out_pos ? p.out_pos[j] : j, B)];
     if (p.post) val = mulv(val, ((const E *)p.post)[r], false);
-    if (p.has_scale) val = mulv(val, scalar_of<E>(p.scale_re, p.scale_im), false);
+    if (p.has_scale) val = mulv(val, c, false);
     if (p.conj_out) val = conjv(val);
     if constexpr (Emu<E>::v) {
       if (p.dst_type == Tr<E>::code && !acc)
