@@ -74,7 +74,12 @@ def _is_dense(m):
 
 
 def _is_param_leaf(m):
-    return isinstance(m, (Diag, Circulant, Toeplitz)) or _is_dense(m)
+    # multi-level Circulant / Toeplitz are applied but not trained
+    if isinstance(m, Circulant):
+        return m.tenC.ndim == 1
+    if isinstance(m, Toeplitz):
+        return m.tenT.ndim == 1
+    return isinstance(m, Diag) or _is_dense(m)
 
 
 def _leaves(m, out=None):

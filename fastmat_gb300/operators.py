@@ -19,6 +19,19 @@ def _squeezed_copy(a):
     return np.squeeze(a).copy() if a.ndim > 1 else a.copy()
 
 
+def _level_diff_matrix(ten, rows, cols):
+    """Dense multi-level difference matrix M[i, j] = ten[((i_k - j_k) mod
+    ten.shape[k])_k], with i = (i_1, ..., i_d) < rows and j < cols
+    enumerated in C order (the block structure of a multi-level circulant,
+    fastmat/Circulant.pyx:344-425, and of the Toeplitz matrices embedded in
+    one, fastmat/Toeplitz.pyx:628-734)."""
+    ri = np.unravel_index(np.arange(int(np.prod(rows))), rows)
+    ci = np.unravel_index(np.arange(int(np.prod(cols))), cols)
+    idx = tuple((r[:, None] - c[None, :]) % n
+                for r, c, n in zip(ri, ci, ten.shape))
+    return ten[idx]
+
+
 class Fourier(Matrix):
     """Unnormalised DFT matrix F[n, k] = exp(-2 pi i n k / N)
     (fastmat/Fourier.pyx:26-285).  ``_numL`` is fastmat's Bluestein length
@@ -336,7 +349,8 @@ class Kron(Matrix):
 
 class Circulant(Partial):
     """Circulant matrix C[i, j] = c[(i - j) mod n]
-    (fastmat/Circulant.pyx:32-227).  The GPU convolves with the FFT of the
+    (fastmat/Circulant.pyx:32-227); a d-dimensional tenC defines a d-level
+    circulant.  The GPU convolves with the FFT of the
     defining vector; ``content`` builds fastmat's Fourier-domain structure
     (Partial of Product(F.H, Diag(fft(c)/L), F)) on demand."""
 
@@ -344,15 +358,13 @@ class Circulant(Partial):
         c = _squeezed_copy(tenC)
         if np.ndim(tenC) < 1 or c.ndim < 1:
             raise ValueError("Column-definition tensor must be at least 1D.")
-        if c.ndim > 1:
-            raise NotImplementedError(
-                "multi-level Circulant is not supported by fastmat_gb300")
         self._optimize = options.get('optimize', True)
         self._maxStage = options.get('maxStage', 4)
         self._tenC = c.astype(np.complex128)
         self._rowSelection = None
         self._colSelection = None
         self._structure = None
+        self._ml = None
         opts = {k: v for k, v in options.items()
                 if k not in ('optimize', 'maxStage', 'rows', 'cols')}
         self._init_properties(c.size, c.size, np.complex128, **opts)
@@ -365,8 +377,25 @@ class Circulant(Partial):
     def vecC(self):
         return self._tenC
 
+    def _multilevel(self):
+        """Multi-level circulant (fastmat/Circulant.pyx:138-215) as
+        Kron(F_n1, ..., F_nd)^H diag(fftn(tenC) / N) Kron(F_n1, ..., F_nd):
+        block (i, j) of level k uses tenC[.., (i - j) mod n_k, ..].  The
+        spectrum is computed on the GPU by the same Kron of Fouriers."""
+        if self._ml is None:
+            dims = self._tenC.shape
+            prec = self._precision
+            KF = Kron(*[Fourier(int(n)) for n in dims])
+            spec = KF.forward(self._tenC.reshape(-1)) / self._tenC.size
+            KFp = Kron(*[Fourier(int(n)) for n in dims], precision=prec)
+            self._ml = Product(Hermitian(KFp), Diag(spec, precision=prec),
+                               KFp, precision=prec)
+        return self._ml
+
     @property
     def content(self):
+        if self._tenC.ndim > 1:
+            return (self._multilevel(),)
         if self._structure is None:
             n = self._tenC.size
             L = fftsize.circulant_length(n, self._optimize, self._maxStage)
@@ -388,16 +417,17 @@ class Circulant(Partial):
         return np.arange(self.numCols)
 
     def _emit(self, b):
+        if self._tenC.ndim > 1:
+            return self._multilevel()._emit(b)
         return b.add(_native.NODE_CIRCULANT, self, vec0=self._tenC)
 
     def _reference(self):
-        n = self._tenC.size
-        i = np.arange(n)
-        return self._tenC[(i[:, None] - i[None, :]) % n].astype(self.dtype)
+        return _level_diff_matrix(self._tenC, self._tenC.shape,
+                                  self._tenC.shape).astype(self.dtype)
 
 
 class Toeplitz(Partial):
-    """Toeplitz matrix (fastmat/Toeplitz.pyx:31-734), 1-level.
+    """Toeplitz matrix (fastmat/Toeplitz.pyx:31-734), one or more levels.
 
     ``Toeplitz(vecC, vecR)``: first column vecC and first row
     [vecC[0], vecR[-1], vecR[-2], ...] (T[0, j] = vecR[-j]);
@@ -423,11 +453,11 @@ class Toeplitz(Partial):
             vr = vr.reshape(-1)
             tenT = np.hstack((vc, vr))
             split = vc.size
+        elif len(args) == 1 and np.ndim(args[0]) > 1:
+            self._init_multilevel(np.asarray(args[0]), split, options)
+            return
         elif len(args) == 1:
             tenT = np.asarray(args[0])
-            if tenT.ndim != 1:
-                raise NotImplementedError(
-                    "multi-level Toeplitz is not supported by fastmat_gb300")
             if split is None:
                 if (tenT.size + 1) % 2 != 0:
                     raise ValueError(
@@ -444,6 +474,7 @@ class Toeplitz(Partial):
                 "one or two fixed arguments")
         self._tenT = tenT.astype(np.complex128)
         self._split = split
+        self._ml = None
         nr = split
         nc = tenT.size - nr + 1
         self._optimize = options.get('optimize', True)
@@ -453,6 +484,61 @@ class Toeplitz(Partial):
         opts = {k: v for k, v in options.items()
                 if k not in ('optimize', 'maxStage', 'rows', 'cols')}
         self._init_properties(nr, nc, np.complex128, **opts)
+
+    def _init_multilevel(self, tenT, split, options):
+        """Multi-level Toeplitz (fastmat/Toeplitz.pyx:180-322): level k has
+        split[k] rows and tenT.shape[k] - split[k] + 1 columns, and
+        T[i, j] = tenT[((i_k - j_k) mod tenT.shape[k])_k] -- the rows with
+        i_k < split[k] and columns with j_k < cols[k] of the multi-level
+        circulant of tenT, which is how it is applied."""
+        dims = np.array(tenT.shape)
+        sp = np.atleast_1d(np.array([] if split is None else split))
+        if sp.size == 0:
+            if not all((d + 1) % 2 == 0 for d in dims):
+                raise ValueError(
+                    "Defining a tensor with non-square levels requires " +
+                    "explicit split points.")
+            sp = (dims + 1) // 2
+        if sp.ndim != 1:
+            raise ValueError("The split point vector must be 1D")
+        if sp.size != tenT.ndim:
+            raise ValueError(
+                "The split point vector must have one entry for each " +
+                "dimension of the defining tensor")
+        if any(v < 1 or v > dims[i] for i, v in enumerate(sp)):
+            raise ValueError(
+                "Entry in split vector outside of defining tensor bounds")
+        self._tenT = tenT.astype(np.complex128)
+        self._split = sp.astype(np.int64)
+        self._rows_lv = tuple(int(v) for v in sp)
+        self._cols_lv = tuple(int(d - v + 1) for d, v in zip(dims, sp))
+        self._optimize = options.get('optimize', True)
+        self._maxStage = options.get('maxStage', 4)
+        self._rowSelection = None
+        self._colSelection = None
+        self._ml = None
+        opts = {k: v for k, v in options.items()
+                if k not in ('optimize', 'maxStage', 'rows', 'cols')}
+        self._init_properties(int(np.prod(self._rows_lv)),
+                              int(np.prod(self._cols_lv)), np.complex128,
+                              **opts)
+
+    def _multilevel(self):
+        if self._ml is None:
+            dims = self._tenT.shape
+
+            def sel(lv):
+                idx = np.unravel_index(np.arange(int(np.prod(dims))), dims)
+                keep = np.ones(int(np.prod(dims)), dtype=bool)
+                for k, n in enumerate(lv):
+                    keep &= idx[k] < n
+                return np.arange(int(np.prod(dims)))[keep]
+
+            C = Circulant(self._tenT, precision=self._precision)
+            self._ml = Partial(C, rows=sel(self._rows_lv),
+                               cols=sel(self._cols_lv),
+                               precision=self._precision)
+        return self._ml
 
     @property
     def tenT(self):
@@ -468,6 +554,8 @@ class Toeplitz(Partial):
 
     @property
     def content(self):
+        if self._tenT.ndim > 1:
+            return (self._multilevel(),)
         raise NotImplementedError(
             "Toeplitz content structure is not materialised by "
             "fastmat_gb300")
@@ -481,10 +569,15 @@ class Toeplitz(Partial):
         return np.arange(self.numCols)
 
     def _emit(self, b):
+        if self._tenT.ndim > 1:
+            return self._multilevel()._emit(b)
         return b.add(_native.NODE_TOEPLITZ, self, vec0=self.vecC,
                      vec1=self.vecR)
 
     def _reference(self):
+        if self._tenT.ndim > 1:
+            return _level_diff_matrix(self._tenT, self._rows_lv,
+                                      self._cols_lv).astype(self.dtype)
         nr, nc = self.shape
         d = np.arange(nr)[:, None] - np.arange(nc)[None, :]
         full = np.concatenate([self.vecR, self.vecC])

@@ -532,12 +532,19 @@ def Transpose(mat):
 
 
 class Circulant(Op):
-    """1-level circulant (fastmat/Circulant.pyx:63-137, 217-227, 344-425).
+    """Circulant; a multi-dimensional c gives the multi-level CirculantML.
+
+    1-level circulant (fastmat/Circulant.pyx:63-137, 217-227, 344-425).
 
     C[i, j] = c[(i - j) mod n].  Forward pads to the embedding length L when
     that is cheaper, convolves via FFT with spectrum fft(c_pad) / L and
     truncates back to n rows.
     """
+
+    def __new__(cls, c, *args, **kw):
+        if np.ndim(np.squeeze(np.asarray(c))) > 1:
+            return CirculantML(np.squeeze(np.asarray(c)))
+        return super().__new__(cls)
 
     def __init__(self, c, optimize=True, max_stage=4):
         self.c = np.array(c).reshape(-1)
@@ -580,7 +587,19 @@ class Toeplitz(Op):
     a circulant of length L >= n_r + n_c - 1 with zeros inserted at the split.
     """
 
-    def __init__(self, vecC, vecR, optimize=True, max_stage=4):
+    def __new__(cls, vecC, vecR=None, *args, split=None, **kw):
+        if vecR is None and np.ndim(vecC) > 1:
+            return ToeplitzML(vecC, split)
+        return super().__new__(cls)
+
+    def __init__(self, vecC, vecR=None, optimize=True, max_stage=4,
+                 split=None):
+        if vecR is None:
+            # one-level tensor form: tenT = [vecC, vecR] split at `split`
+            t = np.asarray(vecC).reshape(-1)
+            sp = (t.size + 1) // 2 if split is None else int(
+                np.atleast_1d(split)[0])
+            vecC, vecR = t[:sp], t[sp:]
         dt = np.promote_types(np.asarray(vecC).dtype, np.asarray(vecR).dtype)
         self.vecC = np.asarray(vecC).astype(dt).reshape(-1)
         self.vecR = np.asarray(vecR).astype(dt).reshape(-1)
@@ -613,6 +632,88 @@ class Toeplitz(Op):
         d = i - j
         full = np.concatenate([self.vecR, self.vecC])  # index d + nc - 1
         return full[d + self.nc - 1].astype(np.complex128)
+
+
+class CirculantML(Op):
+    """Multi-level circulant (fastmat/Circulant.pyx:138-215, 344-425):
+    C[i, j] = c[((i_k - j_k) mod n_k)_k] with row / column indices in C
+    order.  fastmat applies Kron(F_n1, ..., F_nd)^H diag(fftn(c) / N)
+    Kron(F_n1, ..., F_nd) (its per-level zero padding only changes the FFT
+    lengths, not the result); restated with numpy's fftn over the level
+    axes of every column."""
+
+    def __init__(self, c):
+        self.c = np.asarray(c)
+        self.dims = self.c.shape
+        n = int(np.prod(self.dims))
+        self.spectrum = np.fft.fftn(self.c.astype(np.complex128))
+        self.shape = (n, n)
+        self.dtype = np.complex128
+
+    def _apply(self, x, spec):
+        m = x.shape[1]
+        axes = tuple(range(1, len(self.dims) + 1))
+        X = x.T.reshape((m,) + self.dims).astype(np.complex128)
+        Y = np.fft.ifftn(spec[None] * np.fft.fftn(X, axes=axes), axes=axes)
+        return Y.reshape(m, -1).T
+
+    def _fwd(self, x):
+        return self._apply(x, self.spectrum)
+
+    def _bwd(self, x):
+        return self._apply(x, np.conj(self.spectrum))
+
+    def dense(self):
+        return level_diff(self.c, self.dims, self.dims).astype(np.complex128)
+
+
+class ToeplitzML(Op):
+    """Multi-level Toeplitz (fastmat/Toeplitz.pyx:180-322, 628-734): level
+    k has split[k] rows and shape[k] - split[k] + 1 columns and
+    T[i, j] = t[((i_k - j_k) mod shape[k])_k]; fastmat applies it as the
+    matching rows and columns of the multi-level circulant of t."""
+
+    def __init__(self, t, split=None):
+        self.t = np.asarray(t)
+        dims = np.array(self.t.shape)
+        sp = (dims + 1) // 2 if split is None else np.asarray(split)
+        self.rows = tuple(int(v) for v in sp)
+        self.cols = tuple(int(d - v + 1) for d, v in zip(dims, sp))
+        self.circ = CirculantML(self.t)
+        n = int(np.prod(dims))
+        idx = np.unravel_index(np.arange(n), self.t.shape)
+        keep_r = np.ones(n, bool)
+        keep_c = np.ones(n, bool)
+        for k in range(len(dims)):
+            keep_r &= idx[k] < self.rows[k]
+            keep_c &= idx[k] < self.cols[k]
+        self.sel_r = np.arange(n)[keep_r]
+        self.sel_c = np.arange(n)[keep_c]
+        self.n = n
+        self.shape = (self.sel_r.size, self.sel_c.size)
+        self.dtype = np.complex128
+
+    def _fwd(self, x):
+        buf = np.zeros((self.n, x.shape[1]), np.complex128)
+        buf[self.sel_c] = x
+        return self.circ._fwd(buf)[self.sel_r]
+
+    def _bwd(self, x):
+        buf = np.zeros((self.n, x.shape[1]), np.complex128)
+        buf[self.sel_r] = x
+        return self.circ._bwd(buf)[self.sel_c]
+
+    def dense(self):
+        return level_diff(self.t, self.rows, self.cols).astype(np.complex128)
+
+
+def level_diff(ten, rows, cols):
+    """M[i, j] = ten[((i_k - j_k) mod ten.shape[k])_k] for multi-indices
+    i < rows, j < cols in C order (fastmat/Circulant.pyx:349-425)."""
+    ri = np.unravel_index(np.arange(int(np.prod(rows))), rows)
+    ci = np.unravel_index(np.arange(int(np.prod(cols))), cols)
+    return ten[tuple((r[:, None] - c[None, :]) % n
+                     for r, c, n in zip(ri, ci, ten.shape))]
 
 
 class Dense(Op):

@@ -139,6 +139,21 @@ def cases():
         {'c': cplx(rng, 64), 'd': cplx(rng, 64),
          'r': np.sort(rng.choice(64, 16, replace=False))}, dense=False)
     add('dense_matrix', 'Matrix(a)', {'a': cplx(rng, 6, 9)})
+    # multi-level Circulant and Toeplitz (fastmat/Circulant.pyx:138-215,
+    # fastmat/Toeplitz.pyx:180-322)
+    add('circulant_ml_3x4', 'Circulant(cm)', {'cm': cplx(rng, 3, 4)})
+    add('circulant_ml_2x3x5', 'Circulant(cm)', {'cm': cplx(rng, 2, 3, 5)})
+    add('circulant_ml_real', 'Circulant(cm)',
+        {'cm': rng.standard_normal((4, 6))}, xdtype=np.float64)
+    add('circulant_ml_8x16', 'Circulant(cm)', {'cm': cplx(rng, 8, 16)})
+    add('circulant_ml_7x9', 'Circulant(cm)', {'cm': cplx(rng, 7, 9)},
+        dense=False)
+    add('toeplitz_ml_split', 'Toeplitz(tm, split=sp)',
+        {'tm': cplx(rng, 3, 5), 'sp': np.array([2, 3])})
+    add('toeplitz_ml_cube', 'Toeplitz(tm)', {'tm': cplx(rng, 3, 5, 3)})
+    add('toeplitz_ml_rect', 'Toeplitz(tm, split=sp)',
+        {'tm': cplx(rng, 4, 3), 'sp': np.array([4, 1])})
+    add('toeplitz_ml_9x7', 'Toeplitz(tm)', {'tm': cplx(rng, 9, 7)})
     return out
 
 

@@ -251,3 +251,28 @@ def test_kron_with_tensor_core_hadamard_mode():
     y = op.forward(x)
     assert y.dtype == np.float32
     assert fo.rel_err(y, oop.forward(x.astype(np.float64))) <= 1e-5
+
+
+@pytest.mark.parametrize('dims', [(64, 128), (16, 9, 32), (127, 8)])
+def test_multilevel_circulant_large(dims):
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(sum(dims))
+    c = cplx(rng, *dims)
+    C = fg.Circulant(c)
+    oc = fo.Circulant(c)
+    x = cplx(rng, C.numCols, 3)
+    assert fo.rel_err(C.forward(x), oc.forward(x)) <= 1e-12
+    assert fo.rel_err(C.backward(x), oc.backward(x)) <= 1e-12
+
+
+def test_multilevel_toeplitz_large():
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(21)
+    t = cplx(rng, 63, 31)
+    T = fg.Toeplitz(t, split=np.array([40, 20]))
+    ot = fo.Toeplitz(t, split=np.array([40, 20]))
+    assert T.shape == ot.shape == (800, 24 * 12)
+    x = cplx(rng, T.numCols, 2)
+    g = cplx(rng, T.numRows, 2)
+    assert fo.rel_err(T.forward(x), ot.forward(x)) <= 1e-12
+    assert fo.rel_err(T.backward(g), ot.backward(g)) <= 1e-12
