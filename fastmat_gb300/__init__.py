@@ -9,6 +9,7 @@ from .matrix import Conjugate, Hermitian, Matrix, Transpose
 from .operators import (Circulant, Diag, Eye, Fourier, Hadamard, Kron,
                         Partial, Permutation, Product, Sum, Toeplitz)
 from . import _native
+from . import algorithms
 from .batch import Batch
 from ._build import build
 

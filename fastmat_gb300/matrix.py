@@ -355,11 +355,12 @@ class Matrix:
         out_dt = np.dtype(self._output_dtype(in_dt))
         if flat:
             xc = x.contiguous()
-        elif x.stride(0) == 1 and x.stride(1) >= n_req:
+        elif x.stride(0) == 1 and (M == 1 or x.stride(1) >= n_req):
             xc = x
         else:
             xc = x.t().contiguous().t()
-        ld_x = n_req if flat else xc.stride(1)
+        # one column: its stride along the (size-1) column axis is irrelevant
+        ld_x = n_req if (flat or M == 1) else xc.stride(1)
         yt = torch.empty((M, n_out), dtype=_torch_dtype(out_dt),
                          device=x.device)
         if M > 0:
@@ -370,6 +371,42 @@ class Matrix:
                              _native.DTYPE_CODE[in_dt], ld_x, yt.data_ptr(),
                              _native.DTYPE_CODE[out_dt], n_out, M, stream)
         return yt.reshape(n_out) if flat else yt.t()
+
+    # ------------------------------------------------------------ callers
+    @property
+    def largestSingularValue(self):
+        """sigma_max of the operator, as fastmat computes it
+        (fastmat/Matrix.pyx:826-921): scipy's svds (ARPACK) on the
+        LinearOperator, whose matvecs run on the GPU; a dense SVD for
+        operators with at most two rows or columns.  Cached."""
+        v = getattr(self, '_largestSingularValue', None)
+        if v is None:
+            if self.numRows > 2 and self.numCols > 2:
+                from scipy.sparse.linalg import LinearOperator, svds
+                op = LinearOperator(
+                    shape=self.shape, matvec=self.forward,
+                    rmatvec=self.backward, matmat=self.forward,
+                    dtype=np.promote_types(np.float64, self.dtype))
+                v = float(svds(op, 1, return_singular_vectors=False)[0])
+            else:
+                v = float(np.linalg.svd(np.atleast_2d(self.array),
+                                        compute_uv=False)[0])
+            self._largestSingularValue = v
+        return v
+
+    @property
+    def scipyLinearOperator(self):
+        """scipy.sparse.linalg.LinearOperator whose matvec / rmatvec /
+        matmat are this operator's forward / backward
+        (fastmat/Matrix.pyx:985-1006)."""
+        op = getattr(self, '_scipyLinearOperator', None)
+        if op is None:
+            from scipy.sparse.linalg import LinearOperator
+            op = LinearOperator(shape=self.shape, matvec=self.forward,
+                                rmatvec=self.backward, matmat=self.forward,
+                                dtype=self.dtype)
+            self._scipyLinearOperator = op
+        return op
 
     # ------------------------------------------------------------ dense
     def reference(self):
