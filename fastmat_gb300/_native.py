@@ -72,7 +72,8 @@ class FmPlanInfo(ctypes.Structure):
 #: every entry point include/fmgpu.h declares
 EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
            'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
-           'fm_plan_set_tile', 'fm_plan_get_tile', 'fm_plan_autotune',
+           'fm_plan_set_tile', 'fm_plan_set_tile_layout', 'fm_plan_get_tile',
+           'fm_plan_autotune',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
            'fm_batch_create', 'fm_batch_execute', 'fm_batch_execute_graph',
            'fm_batch_check', 'fm_batch_get_info', 'fm_batch_destroy',
@@ -120,6 +121,8 @@ def load(build_if_missing=True):
         lib.fm_execute_host.restype = ctypes.c_int
         lib.fm_plan_set_tile.argtypes = [P, I32, I32, I32, I32]
         lib.fm_plan_set_tile.restype = ctypes.c_int
+        lib.fm_plan_set_tile_layout.argtypes = [P, I32, I32, I32, I32, I32]
+        lib.fm_plan_set_tile_layout.restype = ctypes.c_int
         lib.fm_plan_get_tile.argtypes = [P, I32, I32, ctypes.POINTER(I32),
                                          ctypes.POINTER(I32),
                                          ctypes.POINTER(I32)]
@@ -232,8 +235,10 @@ class Plan:
         return out
 
     def set_tiles(self, direction, tiles):
-        for k, (b, n, _lay) in enumerate(tiles):
-            check(self._lib.fm_plan_set_tile(self.handle, direction, k, b, n))
+        """Replay [(vectors_per_tile, nbuf, layout)] (as tiles() returns)."""
+        for k, (b, n, lay) in enumerate(tiles):
+            check(self._lib.fm_plan_set_tile_layout(self.handle, direction, k,
+                                                    b, n, lay))
 
     def num_launches(self, direction):
         inf = self.info()

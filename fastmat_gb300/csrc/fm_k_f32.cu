@@ -1,87 +1,32 @@
-// Instantiations of the vector-program kernel for element type float.
-#include <map>
-#include <mutex>
-#include <tuple>
-
-#include "fm_launch.cuh"
+// Instantiations of the vector-program kernel for element type float:
+// padded vector-major (layout 0) and element-major (layout 1) tiles; the
+// dense vector-major ones (layout 2) live in fm_k_f32_d.cu so that the two
+// halves compile in parallel.
+#include "fm_klaunch.cuh"
 
 namespace fmk {
 
-template <class K> static cudaError_t cfg(K kernel) {
-  return cudaFuncSetAttribute(kernel,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              kMaxSmem);
-}
+KFn pick_f32_dense(int cls);
 
-template <class K>
-static cudaError_t occ(K kernel, int threads, size_t smem, int *n) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, threads,
-                                                       smem);
+namespace {
+KFn pick_main(int cls, int lay) {
+  switch (cls * 3 + lay) {
+    case 0: return vprog_kernel<float, 0, 0>;
+    case 9: return vprog_kernel<float, 3, 0>;
+    case 10: return vprog_kernel<float, 3, 1>;
+    case 12: return vprog_kernel<float, 4, 0>;
+    case 13: return vprog_kernel<float, 4, 1>;
+    default: return nullptr;
+  }
 }
+}  // namespace
 
-// cls: op subset, lay: tile layout (instantiated pairs only; others run the
-// general vector-major kernel)
 cudaError_t launch_f32(const Step &st, int cls, int lay, int threads,
-                       size_t smem, i64 grid, cudaStream_t s) {
-  static std::mutex mu;
-  static bool configured = false;
-  static int sms = 0;
-  static std::map<std::tuple<int, int, size_t>, int> resident;
-  const int key2 = cls * 2 + lay;
-  int per_sm = 0;
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    cudaError_t e;
-    if (!configured) {
-      if ((e = cfg(vprog_kernel<float, 0, 0>)) != cudaSuccess) return e;
-      if ((e = cfg(vprog_kernel<float, 3, 0>)) != cudaSuccess) return e;
-      if ((e = cfg(vprog_kernel<float, 3, 1>)) != cudaSuccess) return e;
-      if ((e = cfg(vprog_kernel<float, 4, 0>)) != cudaSuccess) return e;
-      if ((e = cfg(vprog_kernel<float, 4, 1>)) != cudaSuccess) return e;
-      int dev = 0;
-      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
-                                      dev)) != cudaSuccess)
-        return e;
-      configured = true;
-    }
-    const auto key = std::make_tuple(key2, threads, smem);
-    auto it = resident.find(key);
-    if (it == resident.end()) {
-      int n = 0;
-      switch (key2) {
-        case 6: e = occ(vprog_kernel<float, 3, 0>, threads, smem, &n); break;
-        case 7: e = occ(vprog_kernel<float, 3, 1>, threads, smem, &n); break;
-        case 8: e = occ(vprog_kernel<float, 4, 0>, threads, smem, &n); break;
-        case 9: e = occ(vprog_kernel<float, 4, 1>, threads, smem, &n); break;
-        default: e = occ(vprog_kernel<float, 0, 0>, threads, smem, &n); break;
-      }
-      if (e != cudaSuccess) return e;
-      it = resident.emplace(key, n < 1 ? 1 : n).first;
-    }
-    per_sm = it->second;
-  }
-  // persistent CTAs: at most as many as fit on the device at once
-  const i64 cap = (i64)per_sm * sms;
-  const i64 g = grid < cap ? grid : cap;
-  switch (key2) {
-    case 6:
-      vprog_kernel<float, 3, 0><<<(unsigned)g, threads, smem, s>>>(st);
-      break;
-    case 7:
-      vprog_kernel<float, 3, 1><<<(unsigned)g, threads, smem, s>>>(st);
-      break;
-    case 8:
-      vprog_kernel<float, 4, 0><<<(unsigned)g, threads, smem, s>>>(st);
-      break;
-    case 9:
-      vprog_kernel<float, 4, 1><<<(unsigned)g, threads, smem, s>>>(st);
-      break;
-    default:
-      vprog_kernel<float, 0, 0><<<(unsigned)g, threads, smem, s>>>(st);
-      break;
-  }
-  return cudaGetLastError();
+                      size_t smem, i64 grid, cudaStream_t s) {
+  const KFn fn = lay == 2 ? pick_f32_dense(cls) : pick_main(cls, lay);
+  // no fallback to another layout: the planner only picks instantiated ones
+  if (!fn) return cudaErrorInvalidConfiguration;
+  return launch_kfn(fn, st, threads, smem, grid, s);
 }
 
 }  // namespace fmk

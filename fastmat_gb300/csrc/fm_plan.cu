@@ -317,7 +317,8 @@ fmk::Op mkop(int kind, int len) {
 // heuristic choice; explicit values (the autotuner's candidates) are
 // accepted when feasible.  Returns false if the request cannot be met.
 bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
-               bool allow_em = true) {
+               bool allow_em = true, int want_lay = -1,
+               bool allow_dense = true) {
   fmk::Step &st = ls.st;
   const int L = std::max(st.L, 1);
   const int ept = ls.ept;
@@ -346,8 +347,11 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   // element-major tiles: strided input and output views whose inner extent
   // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
   // budget allows, never below 16 B), moved by TMA boxes
-  if (allow_em && (ls.cls == 1 || ls.cls == 3 || ls.cls == 4) &&
-      st.vin.Cc > 1 &&
+  if (want_lay == 1 && !(allow_em && (ls.cls == 1 || ls.cls == 3 ||
+                                      ls.cls == 4)))
+    return false;
+  if (allow_em && (want_lay == -1 || want_lay == 1) &&
+      (ls.cls == 1 || ls.cls == 3 || ls.cls == 4) && st.vin.Cc > 1 &&
       st.vout.Cc > 1) {
     int B = want_B ? want_B : 128 / esz;
     if (!want_B) {
@@ -376,18 +380,32 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
         return true;
       }
     }
-    if (want_B) return false;
+    if (want_B || want_lay == 1) return false;
   }
+  if (want_lay == 1) return false;
 
-  // vector-major tiles, padded: one 16-byte granule per 128 bytes (pidx),
-  // rounded to whole granules, with an odd granule count so that
-  // consecutive vectors start on different banks
+  // vector-major tiles.  Padded (layout 0): one 16-byte granule per 128
+  // bytes (pidx), rounded to whole granules, with an odd granule count so
+  // that consecutive vectors start on different banks.  Dense (layout 2):
+  // vectors back to back, so that runs of contiguous vectors move as single
+  // bulk copies; chosen for contiguous vectors whose program has no
+  // butterfly stages (bank conflicts only matter there), or when asked.
+  const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
+  bool stages = false;
+  for (int o = 0; o < st.nops; ++o)
+    if (st.ops[o].kind == fmk::OP_DIF || st.ops[o].kind == fmk::OP_DIT ||
+        st.ops[o].kind == fmk::OP_FWHT)
+      stages = true;
+  const bool dense_ok = allow_dense && !strided && want_lay != 0;
+  if (want_lay == 2 && !dense_ok) return false;
+  if (want_lay > 2) return false;
+  const bool dense = dense_ok && (want_lay == 2 || !stages);
   const int shift = esz >= 16 ? 3 : (esz == 8 ? 4 : 5);
   const int gran = 16 / esz;
   int Lp = (L - 1) + gran * ((L - 1) >> shift) + 1;
   Lp = (Lp + gran - 1) / gran * gran;
   if (((Lp / gran) & 1) == 0) Lp += gran;
-  const bool strided = st.vin.Cc > 1 || st.vout.Cc > 1;
+  if (dense) Lp = L;
   auto smem_for = [&](int b, int nb) {
     return lsmem(b, Lp, nb);
   };
@@ -408,7 +426,7 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   const int nbuf = pick_nbuf(B, Lp);
   const size_t smem = smem_for(B, nbuf);
   if (smem > (size_t)fmk::kMaxSmem) return false;
-  ls.lay = 0;
+  ls.lay = dense ? 2 : 0;
   st.B = B;
   st.Lp = Lp;
   st.nbuf = nbuf;
@@ -422,7 +440,7 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
                  !st.map_in && st.in_rows == st.vin.A * st.vin.n &&
                  ((i64)st.in_len * esz) % 16 == 0;
   ls.tma_out_ok = FM_VM_BULK && st.vout.Cc == 1 &&
-                  st.out_len == st.vout.n &&
+                  st.out_len == st.vout.n && (!dense || st.out_len == L) &&
                   st.out_mode == 0 && !st.accumulate &&
                   st.out_rows == st.vout.A * st.vout.n &&
                   ((i64)st.out_len * esz) % 16 == 0;
@@ -1655,7 +1673,7 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
   st.err = P->err;
   st.tma_in = st.tma_out = 0;
-  if (ls.lay == 0) {
+  if (ls.lay == 0 || ls.lay == 2) {
     const int esz = P->esz;
     auto aligned = [&](const void *ptr, i64 ld, i64 n) {
       return ((uintptr_t)ptr & 15) == 0 && (ld * esz) % 16 == 0 &&
@@ -2062,10 +2080,33 @@ int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,
       fail(FM_ERR_VALUE, "launch index out of range");
     LStep &ls = steps[launch];
     const LStep keep = ls;
-    if (!configure(plan->esz, ls, vectors_per_tile, nbuf)) {
+    if (!configure(plan->esz, ls, vectors_per_tile, nbuf, true, ls.lay)) {
       ls = keep;
       fail(FM_ERR_VALUE, "tile configuration not feasible for this launch");
     }
+    ls.tm_in_key = ls.tm_out_key = nullptr;  // boxes follow the tile shape
+    return FM_OK;
+  });
+}
+
+int fm_plan_set_tile_layout(fm_plan *plan, int32_t direction, int32_t launch,
+                            int32_t vectors_per_tile, int32_t nbuf,
+                            int32_t layout) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (direction != FM_FORWARD && direction != FM_BACKWARD)
+      fail(FM_ERR_VALUE, "invalid direction");
+    std::vector<LStep> &steps = plan->steps[direction];
+    if (launch < 0 || launch >= (int)steps.size())
+      fail(FM_ERR_VALUE, "launch index out of range");
+    if (layout < 0 || layout > 2) fail(FM_ERR_VALUE, "invalid layout");
+    LStep &ls = steps[launch];
+    const LStep keep = ls;
+    if (!configure(plan->esz, ls, vectors_per_tile, nbuf, true, layout)) {
+      ls = keep;
+      fail(FM_ERR_VALUE, "tile configuration not feasible for this launch");
+    }
+    ls.tm_in_key = ls.tm_out_key = nullptr;
     return FM_OK;
   });
 }
@@ -2119,11 +2160,12 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
         CUDA_TRY(cudaMemsetAsync(tdst, 0x3F, (size_t)(rd * M * plan->esz), s));
         const LStep base = ls;
         float best = 1e30f;
-        int bestB = base.st.B, bestN = base.st.nbuf;
+        int bestB = base.st.B, bestN = base.st.nbuf, bestL = base.lay;
+        for (int lay : {1, 0, 2})
         for (int B = 1; B <= 1024; B *= 2) {
           for (int nb = 2; nb <= 4; ++nb) {
             ls = base;
-            if (!configure(plan->esz, ls, B, nb)) continue;
+            if (!configure(plan->esz, ls, B, nb, true, lay)) continue;
             fmk::Step st = ls.st;
             st.src = tsrc;
             st.dst = tdst;
@@ -2146,11 +2188,12 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
               best = t;
               bestB = B;
               bestN = nb;
+              bestL = lay;
             }
           }
         }
         ls = base;
-        if (!configure(plan->esz, ls, bestB, bestN)) ls = base;
+        if (!configure(plan->esz, ls, bestB, bestN, true, bestL)) ls = base;
         ls.tm_in_key = ls.tm_out_key = nullptr;  // descriptors of the temps
         cudaFree(tsrc);
         cudaFree(tdst);
@@ -2318,7 +2361,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
       int level = 0;
       for (const LStep &ls0 : P->steps[dir]) {
         LStep ls = ls0;
-        if (!configure(esz, ls, 0, 0, false))
+        if (!configure(esz, ls, 0, 0, false, 0, false))
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "
                                    "vector-major tile shape");
         fmk::Step st = ls.st;
@@ -2496,6 +2539,6 @@ int fm_batch_destroy(fm_batch *batch) {
 
 const char *fm_last_error(void) { return g_err.c_str(); }
 
-int32_t fm_version(void) { return 100; }
+int32_t fm_version(void) { return 101; }
 
 }  // extern "C"

@@ -380,9 +380,20 @@ struct VInfo {
 //        bytes (pidx), threads walk the elements of a vector.
 // LAY 1: element-major tile, element j of vector b at j * B + b (dense),
 //        threads walk the vectors first; filled and drained by TMA boxes.
+// LAY 2: vector-major tile without padding (vector b at b * L): contiguous
+//        vectors then move as one bulk copy per run of vectors, at the cost
+//        of bank conflicts for some strided FFT stages (the autotuner picks
+//        between LAY 0 and LAY 2).
 template <class E, int LAY>
 __device__ __forceinline__ int jx(int j, int B) {
   if constexpr (LAY == 1) return j * B;
+  else if constexpr (LAY == 2) return j;
+  else return pidx<E>(j);
+}
+// position of element j inside a vector-major vector (LAY 0 or 2)
+template <class E, int LAY>
+__device__ __forceinline__ int vx(int j) {
+  if constexpr (LAY == 2) return j;
   else return pidx<E>(j);
 }
 template <class E, int LAY>
@@ -637,7 +648,7 @@ __device__ void run_fwht(const Op &op, E *sm, int Lp, int B, int tid, int T,
 
 // ------------------------------------------------------------ other ops
 // (gathers and dense products run on vector-major tiles only)
-template <class E>
+template <class E, int LAY>
 __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
                            int T) {
   constexpr int MB = Ept<E>::v;
@@ -650,7 +661,7 @@ __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
     for (int i = 0; i < MB; ++i, w.next()) {
       if (tid + i * T < total) {
         const i64 src = map[w.j];
-        v[i] = src < 0 ? zero<E>() : sm[w.b * Lp + pidx<E>((int)src)];
+        v[i] = src < 0 ? zero<E>() : sm[w.b * Lp + vx<E, LAY>((int)src)];
       }
     }
   }
@@ -659,12 +670,12 @@ __device__ void run_gather(const Op &op, E *sm, int Lp, int B, int tid,
     Walk w(tid, op.len, T);
 #pragma unroll
     for (int i = 0; i < MB; ++i, w.next())
-      if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
+      if (tid + i * T < total) sm[w.b * Lp + vx<E, LAY>(w.j)] = v[i];
   }
   group_sync(T);
 }
 
-template <class E>
+template <class E, int LAY>
 __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
                           int T) {
   constexpr int MB = Ept<E>::v;
@@ -680,7 +691,7 @@ __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
         const E *vec = sm + w.b * Lp;
         E acc = zero<E>();
         for (int j = 0; j < cols; ++j)
-          acc = addv(acc, mulv(M[w.j + (i64)j * rows], vec[pidx<E>(j)],
+          acc = addv(acc, mulv(M[w.j + (i64)j * rows], vec[vx<E, LAY>(j)],
                                false));
         v[i] = acc;
       }
@@ -691,7 +702,7 @@ __device__ void run_dense(const Op &op, E *sm, int Lp, int B, int tid,
     Walk w(tid, rows, T);
 #pragma unroll
     for (int i = 0; i < MB; ++i, w.next())
-      if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
+      if (tid + i * T < total) sm[w.b * Lp + vx<E, LAY>(w.j)] = v[i];
   }
   group_sync(T);
 }
@@ -710,7 +721,7 @@ __device__ __forceinline__ void ew_loop(E *sm, int Lp, int B, int len,
   } else {
     Walk w(tid, len, T);
     for (int g = tid; g < total; g += T, w.next())
-      f(sm[w.b * Lp + pidx<E>(w.j)], w.b, w.j);
+      f(sm[w.b * Lp + vx<E, LAY>(w.j)], w.b, w.j);
   }
 }
 
@@ -1000,6 +1011,25 @@ __device__ __forceinline__ void issue_load(const Step &p, E *sm, unsigned bar,
                                            int tid, int T) {
   if constexpr (LAY == 1) {
     if (tid == 0) tma_issue_load<E>(p, sm, bar, tile);
+  } else if constexpr (LAY == 2) {
+    // dense tile: every run of consecutive vectors within one column is a
+    // single bulk copy (vector b at b * L, L = in_len)
+    if (tid != 0) return;
+    const i64 gv0 = tile * p.B;
+    const int nv = (int)(nvec - gv0 < p.B ? nvec - gv0 : p.B);
+    const int L = p.in_len;
+    mbar_expect_tx(bar, (unsigned)((size_t)nv * L * sizeof(E)));
+    const E *src = (const E *)p.src;
+    for (int b = 0; b < nv;) {
+      const unsigned g = (unsigned)(gv0 + b);
+      const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
+      int cnt = (int)((unsigned)p.V - v);
+      if (cnt > nv - b) cnt = nv - b;
+      bulk_load(smem_addr(sm + (i64)b * L),
+                src + (i64)m * p.ld_src + (i64)v * p.vin.n,
+                (unsigned)((size_t)cnt * L * sizeof(E)), bar);
+      b += cnt;
+    }
   } else {
     constexpr int CH = 128 / (int)sizeof(E);
     const int nch = (p.in_len + CH - 1) / CH;
@@ -1026,6 +1056,23 @@ __device__ __forceinline__ void issue_store(const Step &p, const E *sm,
                                             i64 nvec, int tid, int T) {
   if constexpr (LAY == 1) {
     if (tid == 0) tma_issue_store<E>(p, sm, tile);
+  } else if constexpr (LAY == 2) {
+    if (tid != 0) return;
+    const i64 gv0 = tile * p.B;
+    const int nv = (int)(nvec - gv0 < p.B ? nvec - gv0 : p.B);
+    const int L = p.out_len;
+    E *dst = (E *)p.dst;
+    for (int b = 0; b < nv;) {
+      const unsigned g = (unsigned)(gv0 + b);
+      const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
+      int cnt = (int)((unsigned)p.V - v);
+      if (cnt > nv - b) cnt = nv - b;
+      bulk_store(dst + (i64)m * p.ld_dst + (i64)v * p.vout.n,
+                 smem_addr(sm + (i64)b * L),
+                 (unsigned)((size_t)cnt * L * sizeof(E)));
+      b += cnt;
+    }
+    bulk_commit();
   } else {
     constexpr int CH = 128 / (int)sizeof(E);
     const int nch = (p.out_len + CH - 1) / CH;
@@ -1050,7 +1097,7 @@ __device__ __forceinline__ void issue_store(const Step &p, const E *sm,
 
 // vector-major tiles before a bulk store: reorder (out_pos), post-multiply,
 // scale, conjugate and (double-float) convert in shared memory
-template <class E>
+template <class E, int LAY>
 __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
                                                const VInfo *vi,
                                                const int *sexp, int tid,
@@ -1065,14 +1112,14 @@ __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
 #pragma unroll
       for (int i = 0; i < MB; ++i, w.next())
         if (tid + i * T < total)
-          v[i] = sm[w.b * Lp + pidx<E>(p.out_pos[w.j])];
+          v[i] = sm[w.b * Lp + vx<E, LAY>(p.out_pos[w.j])];
     }
     __syncthreads();
     {
       Walk w(tid, n, T);
 #pragma unroll
       for (int i = 0; i < MB; ++i, w.next())
-        if (tid + i * T < total) sm[w.b * Lp + pidx<E>(w.j)] = v[i];
+        if (tid + i * T < total) sm[w.b * Lp + vx<E, LAY>(w.j)] = v[i];
     }
     __syncthreads();
   }
@@ -1084,7 +1131,7 @@ __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
   Walk w(tid, n, T);
   for (int f = tid; f < total; f += T, w.next()) {
     const int b = w.b, j = w.j;
-    E *e = sm + b * Lp + pidx<E>(j);
+    E *e = sm + b * Lp + vx<E, LAY>(j);
     E val = *e;
     if (post && vi[b].rb_out >= 0)
       val = mulv(val, post[vi[b].rb_out + j], false);
@@ -1246,7 +1293,7 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
   const int B = p.B, Lp = p.Lp;
   const bool acc = p.accumulate != 0;
   const E c = scalar_of<E>(p.scale_re, p.scale_im);
-  if constexpr (LAY == 0) {
+  if constexpr (LAY != 1) {
     if (p.out_mode == 1) {
       // gather: out row i of column m takes vector element map_out[i]
       Walk w(tid, p.n_out, T);
@@ -1254,7 +1301,7 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
         const int b = w.b, i = w.j;
         if (vi[b].rb_out < 0) continue;
         const i64 j = p.map_out[i];
-        E val = j < 0 ? zero<E>() : sm[b * Lp + pidx<E>((int)j)];
+        E val = j < 0 ? zero<E>() : sm[b * Lp + vx<E, LAY>((int)j)];
         if (j >= 0 && p.post) val = mulv(val, ((const E *)p.post)[j], false);
         if (p.has_scale) val = mulv(val, c, false);
         if (p.conj_out) val = conjv(val);
@@ -1381,12 +1428,12 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
           run_fwht<E, LAY>(op, sm, Lp, B, tid, T, tc);
         break;
       case OP_GATHER:
-        if constexpr (CLS == 0 && LAY == 0)
-          run_gather<E>(op, sm, Lp, B, tid, T);
+        if constexpr (CLS == 0 && LAY != 1)
+          run_gather<E, LAY>(op, sm, Lp, B, tid, T);
         break;
       case OP_DENSE:
-        if constexpr (CLS == 0 && LAY == 0)
-          run_dense<E>(op, sm, Lp, B, tid, T);
+        if constexpr (CLS == 0 && LAY != 1)
+          run_dense<E, LAY>(op, sm, Lp, B, tid, T);
         break;
       case OP_ZPAD: run_zpad<E, LAY>(op, sm, Lp, B, tid, T); break;
       default:
@@ -1421,7 +1468,7 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // program's stages need warp barriers only.
 template <class E, int CLS, int LAY>
 __device__ __forceinline__ bool warp_mode(int B, int L, int nwarps) {
-  return LAY == 0 && CLS != 4 && nwarps > 1 && B % nwarps == 0 &&
+  return LAY != 1 && CLS != 4 && nwarps > 1 && B % nwarps == 0 &&
          (B / nwarps) * L <= 32 * Ept<E>::v;
 }
 
@@ -1557,7 +1604,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
           __syncthreads();
         }
       } else {
-        store_fixup_vm<E>(p, sm, vi, sexp, tid, T);
+        store_fixup_vm<E, LAY>(p, sm, vi, sexp, tid, T);
       }
       // every writer orders its shared-memory writes before the bulk /
       // TMA reads of the store, then the issuing threads start it

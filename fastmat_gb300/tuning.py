@@ -30,8 +30,9 @@ def _key(plan, num_cols):
     h = hashlib.sha1()
     for d in (_native.FORWARD, _native.BACKWARD):
         h.update(plan.describe(d).encode())
-    h.update(('|%d|%d|%s' % (plan.compute_type, num_cols,
-                             _device_name())).encode())
+    h.update(('|%d|%d|%s|%d' % (plan.compute_type, num_cols,
+                                _device_name(),
+                                _native.load().fm_version())).encode())
     return h.hexdigest()
 
 

@@ -193,11 +193,18 @@ int fm_execute_host(fm_plan *plan, int32_t direction,
                     int64_t num_cols);
 
 /* Tile shape of launch `launch` of a direction: vectors per tile and the
- * depth (2..4) of its copy ring; fm_plan_set_tile returns FM_ERR_VALUE for
- * an infeasible request and leaves the launch unchanged.  layout: 0 vector-
- * major, 1 element-major (TMA boxes).  The reference has no counterpart. */
+ * depth (2..4) of its copy ring, keeping the launch's tile layout;
+ * fm_plan_set_tile returns FM_ERR_VALUE for an infeasible request and leaves
+ * the launch unchanged.  layout: 0 vector-major padded, 1 element-major (TMA
+ * boxes), 2 vector-major dense.  The reference has no counterpart. */
 int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,
                      int32_t vectors_per_tile, int32_t nbuf);
+/* Same with the tile layout: 0 vector-major padded, 1 element-major (TMA
+ * boxes; strided views), 2 vector-major dense (contiguous vectors, one bulk
+ * copy per run of vectors). */
+int fm_plan_set_tile_layout(fm_plan *plan, int32_t direction, int32_t launch,
+                            int32_t vectors_per_tile, int32_t nbuf,
+                            int32_t layout);
 int fm_plan_get_tile(const fm_plan *plan, int32_t direction, int32_t launch,
                      int32_t *vectors_per_tile, int32_t *nbuf,
                      int32_t *layout);
