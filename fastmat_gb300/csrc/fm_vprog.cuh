@@ -452,16 +452,18 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
     const int K = (int)dM.div((unsigned)w), t = w - K * M;
     C *vec = vbase<C, LAY>(sm, b, Lp);
     const int base = K * Mprev + t;
+    // twiddle w^(t k) is tw[k * tstep]; for t = 0 it is tw[0] = 1 exactly,
+    // so the products run unconditionally (straight-line code)
+    const C *twt = tw;
+    const int tstep = t * tscale;
     C v[R];
 #pragma unroll
     for (int n = 0; n < R; ++n) v[n] = vec[jx<C, LAY>(base + M * n, B)];
     if constexpr (DIT) {
-      if (t != 0) {
 #pragma unroll
-        for (int k = 1; k < R; ++k) {
-          const C w = tw[t * k * tscale];
-          v[k] = sign < 0 ? cmul(v[k], w) : cmulc(v[k], w);
-        }
+      for (int k = 1; k < R; ++k) {
+        const C w = twt[k * tstep];
+        v[k] = sign < 0 ? cmul(v[k], w) : cmulc(v[k], w);
       }
     }
     if constexpr ((R & (R - 1)) == 0) {
@@ -470,8 +472,8 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
       for (int i = 0; i < R; ++i) {
         C y = v[i];
         if constexpr (!DIT) {
-          if (t != 0 && brev<R>(i) != 0) {
-            const C w = tw[t * brev<R>(i) * tscale];
+          if (brev<R>(i) != 0) {  // folded by the unrolled loop
+            const C w = twt[brev<R>(i) * tstep];
             y = sign < 0 ? cmul(y, w) : cmulc(y, w);
           }
         }
@@ -483,8 +485,8 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
       for (int k = 0; k < R; ++k) {
         C y = v[k];
         if constexpr (!DIT) {
-          if (t != 0 && k != 0) {
-            const C w = tw[t * k * tscale];
+          if (k != 0) {
+            const C w = twt[k * tstep];
             y = sign < 0 ? cmul(y, w) : cmulc(y, w);
           }
         }
