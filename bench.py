@@ -270,22 +270,28 @@ def time_device(torch, op, xt, steps, warmup, barrier):
     return e0.elapsed_time(e1) / steps, yt
 
 
-def _dist_setup(torch, world, local):
-    """(barrier, max-over-ranks) for N replicas (NCCL), no-ops for one."""
+def _dist_setup(torch, world, local, backend=None):
+    """(barrier, max-over-ranks) for N replicas, no-ops for one.  The
+    replicas exchange no data; the process group only times them together
+    (NCCL on GPUs, gloo where there is none)."""
+    cuda = torch.cuda.is_available()
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group('nccl')
+        if cuda:
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend or ('nccl' if cuda else 'gloo'))
+        dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
 
         def barrier():
             dist.barrier()
 
         def allmax(v):
-            t = torch.tensor([v], dtype=torch.float64, device='cuda')
+            t = torch.tensor([v], dtype=torch.float64, device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             return float(t.item())
         return barrier, allmax
-    torch.cuda.set_device(0)
+    if cuda:
+        torch.cuda.set_device(0)
     return (lambda: None), (lambda v: v)
 
 
