@@ -120,28 +120,6 @@ __device__ __forceinline__ df d2df(double d) {
   return df(h, l);
 }
 
-// double-float -> double: widen both floats exactly (bit manipulation) and
-// add once in double precision
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned u = (unsigned)__float_as_int(f);
-  const unsigned long long sg = (unsigned long long)(u >> 31) << 63;
-  const unsigned ex = (u >> 23) & 0xFF;
-  const unsigned long long mt = u & 0x7FFFFF;
-  if (ex == 0) {
-    if (mt == 0) return __longlong_as_double((long long)sg);
-    return (double)f;  // subnormal float: rare, let the hardware widen it
-  }
-  if (ex == 0xFF)
-    return __longlong_as_double(
-        (long long)(sg | 0x7FF0000000000000ull | (mt << 29)));
-  return __longlong_as_double(
-      (long long)(sg | ((unsigned long long)(ex - 127 + 1023) << 52) |
-                  (mt << 29)));
-}
-__device__ __forceinline__ double df2d(df a) {
-  return f2d_exact(a.h) + f2d_exact(a.l);
-}
-
 // ---------------------------------------------------------------- traits
 template <class E> struct Tr;
 template <> struct Tr<float> {
@@ -425,34 +403,6 @@ __device__ __forceinline__ void split(double2 v, double &re, double &im) {
 __device__ __forceinline__ int dexp(double d) {
   return (int)(((unsigned long long)__double_as_longlong(d) >> 52) & 0x7FF);
 }
-// d * 2^-s by exponent arithmetic (results below the normal range flush to
-// zero, above it saturate to infinity)
-__device__ __forceinline__ double dscale(double d, int s) {
-  if (s == 0) return d;
-  unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0 || ex == 0x7FF) return d;
-  const int ne = ex - s;
-  const unsigned long long sg = b & 0x8000000000000000ull;
-  if (ne <= 0) return __longlong_as_double((long long)sg);
-  if (ne >= 0x7FF)
-    return __longlong_as_double((long long)(sg | 0x7FF0000000000000ull));
-  b = (b & ~(0x7FFull << 52)) | ((unsigned long long)ne << 52);
-  return __longlong_as_double((long long)b);
-}
-
-// (double-float values carry their vector's power-of-two scale s)
-__device__ __forceinline__ void split(df v, double &re, double &im,
-                                      int s = 0) {
-  re = dscale(df2d(v), -s);
-  im = 0.;
-}
-__device__ __forceinline__ void split(dfc v, double &re, double &im,
-                                      int s = 0) {
-  re = dscale(df2d(v.x), -s);
-  im = dscale(df2d(v.y), -s);
-}
-
 // in-place conversions of a double-float tile element and its float64 /
 // complex128 bit pattern (same size)
 // (s: power-of-two scale of the vector, removed on load, restored on store)
@@ -464,19 +414,101 @@ __device__ __forceinline__ int raw_exp(dfc raw) {
   const int a = dexp(d.x), b = dexp(d.y);
   return a > b ? a : b;
 }
+// Tile conversions, branch-free (they run once per element on every load
+// and store of the double-float kernels).
+// float64 d times 2^-s -> double-float: h keeps the leading 24 significand
+// bits (truncated), l is the other 29 bits rounded to a float, so h + l is
+// within 2^-48 |d|.  s is the vector's largest exponent minus the bias (so
+// every element's rebased float exponent is at most 127): elements more
+// than 2^126 below that flush to zero, their l more than 2^74 below it;
+// Inf and NaN stay Inf and NaN.
+__device__ __forceinline__ df d2df_scaled(double d, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sg = hi & 0x80000000u;
+  const int ex = (int)((hi >> 20) & 0x7FFu);
+  const int ef = ex - s - 896;  // biased float exponent of h
+  const unsigned mh = __funnelshift_l(lo, hi, 3) & 0x7FFFFFu;
+  float h = __int_as_float((int)(sg | ((unsigned)ef << 23) | mh));
+  // the remaining bits weigh 2^(ef - 127 - 52) each
+  float l = (float)(lo & 0x1FFFFFFFu) * __int_as_float((ef - 52) << 23);
+  l = __int_as_float(__float_as_int(l) | (int)sg);
+  if (ef < 53) l = 0.f;
+  if (ef < 1) h = 0.f;
+  if (ex == 0x7FF) {
+    h = __int_as_float((int)(sg | (((hi & 0xFFFFFu) | lo) ? 0x7FC00000u
+                                                           : 0x7F800000u)));
+    l = 0.f;
+  }
+  return df(h, l);
+}
+// float -> float64, exact for normal floats; zero and subnormal floats give
+// a signed zero, Inf and NaN stay Inf and NaN
+__device__ __forceinline__ double f2d_fast(float f) {
+  const unsigned u = (unsigned)__float_as_int(f);
+  const unsigned ex = (u >> 23) & 0xFFu;
+  // exponent rebased by 1023 - 127 = 896 (0x38000000 = 896 << 20)
+  unsigned hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
+  unsigned lo = u << 29;
+  if (ex == 0) {
+    hi = u & 0x80000000u;
+    lo = 0u;
+  }
+  if (ex == 0xFFu) hi |= 0x7FF00000u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+// d * 2^s by exponent arithmetic: zero, Inf and NaN unchanged, results
+// beyond the float64 range saturate to Inf or flush to a signed zero
+__device__ __forceinline__ double dscale_fast(double d, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int ex = (int)((hi >> 20) & 0x7FFu);
+  const int ne = ex + s;
+  const unsigned sg = hi & 0x80000000u;
+  unsigned nhi = hi + ((unsigned)s << 20), nlo = lo;
+  if (ne <= 0) {
+    nhi = sg;
+    nlo = 0u;
+  }
+  if (ne >= 0x7FF) {
+    nhi = sg | 0x7FF00000u;
+    nlo = 0u;
+  }
+  if (ex == 0 || ex == 0x7FF) {
+    nhi = hi;
+    nlo = lo;
+  }
+  return __hiloint2double((int)nhi, (int)nlo);
+}
+__device__ __forceinline__ double df2d_scaled(df v, int s) {
+  return dscale_fast(f2d_fast(v.h) + f2d_fast(v.l), s);
+}
+
+// (double-float values carry their vector's power-of-two scale s)
+__device__ __forceinline__ void split(df v, double &re, double &im,
+                                      int s = 0) {
+  re = df2d_scaled(v, s);
+  im = 0.;
+}
+__device__ __forceinline__ void split(dfc v, double &re, double &im,
+                                      int s = 0) {
+  re = df2d_scaled(v.x, s);
+  im = df2d_scaled(v.y, s);
+}
+
 __device__ __forceinline__ df from_bits(df raw, int s) {
-  return d2df(dscale(*reinterpret_cast<const double *>(&raw), s));
+  return d2df_scaled(*reinterpret_cast<const double *>(&raw), s);
 }
 __device__ __forceinline__ dfc from_bits(dfc raw, int s) {
   const double2 d = *reinterpret_cast<const double2 *>(&raw);
-  return dfc{d2df(dscale(d.x, s)), d2df(dscale(d.y, s))};
+  return dfc{d2df_scaled(d.x, s), d2df_scaled(d.y, s)};
 }
 __device__ __forceinline__ df to_bits(df v, int s) {
-  const double d = dscale(df2d(v), -s);
+  const double d = df2d_scaled(v, s);
   return *reinterpret_cast<const df *>(&d);
 }
 __device__ __forceinline__ dfc to_bits(dfc v, int s) {
-  const double2 d = make_double2(dscale(df2d(v.x), -s), dscale(df2d(v.y), -s));
+  const double2 d = make_double2(df2d_scaled(v.x, s), df2d_scaled(v.y, s));
   return *reinterpret_cast<const dfc *>(&d);
 }
 
