@@ -5,7 +5,8 @@ Drop-in classes with fastmat's constructors and ``forward``/``backward``/
 (include/fmgpu.h).
 """
 
-from .matrix import Conjugate, Hermitian, Matrix, Transpose
+from .matrix import (Conjugate, Hermitian, Inverse, Matrix, PseudoInverse,
+                     Transpose)
 from .operators import (Circulant, Diag, Eye, Fourier, Hadamard, Kron,
                         Partial, Permutation, Product, Sum, Toeplitz)
 from . import _native
@@ -17,7 +18,8 @@ __version__ = '0.1.0'
 
 __all__ = ['Matrix', 'Hermitian', 'Conjugate', 'Transpose', 'Fourier',
            'Circulant', 'Toeplitz', 'Hadamard', 'Diag', 'Eye', 'Partial',
-           'Permutation', 'Product', 'Sum', 'Kron', 'Batch', 'build']
+           'Permutation', 'Product', 'Sum', 'Kron', 'Inverse', 'PseudoInverse',
+           'Batch', 'build']
 
 
 def native_library():

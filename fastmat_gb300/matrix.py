@@ -408,6 +408,100 @@ class Matrix:
             self._scipyLinearOperator = op
         return op
 
+    @property
+    def largestEigenValue(self):
+        """Eigenvalue of largest magnitude of a square operator
+        (fastmat/Matrix.pyx:680-765): scipy's eigs (ARPACK) on the
+        LinearOperator whose matvecs run on the GPU; numpy's eigvals of the
+        dense array for a 1 x 1 operator.  Cached."""
+        v = getattr(self, '_largestEigenValue', None)
+        if v is None:
+            if self.numRows != self.numCols:
+                raise ValueError("largestEigenValue: Matrix must be square.")
+            if self.numRows > 1:
+                from scipy.sparse.linalg import eigs
+                v = eigs(self._promoted_operator(), 1,
+                         return_eigenvectors=False)[0]
+            else:
+                v = np.linalg.eigvals(self.array)[0]
+            self._largestEigenValue = v
+        return v
+
+    @property
+    def largestEigenVec(self):
+        """Eigenvector of the largest-magnitude eigenvalue
+        (fastmat/Matrix.pyx:771-811).  Cached with the eigenvalue."""
+        v = getattr(self, '_largestEigenVec', None)
+        if v is None:
+            if self.numRows != self.numCols:
+                raise ValueError("largestEigenVec: Matrix must be square.")
+            dt = np.promote_types(np.float64, self.dtype)
+            if self.numRows > 2:
+                from scipy.sparse.linalg import eigs
+                S, V = eigs(self._promoted_operator(), 1,
+                            return_eigenvectors=True)
+                S, v = S[0], V[:, 0]
+            else:
+                S, V = np.linalg.eig(self.array)
+                S, v = S.astype(dt)[0], V[:, 0].astype(dt)
+            self._largestEigenValue = S
+            self._largestEigenVec = v
+        return v
+
+    @property
+    def largestSingularVectors(self):
+        """(u, v) leading left and right singular vectors
+        (fastmat/Matrix.pyx:925-983): scipy's svds over GPU matvecs; a dense
+        SVD for a single row or column.  Cached with the singular value.
+        Real vectors are returned as float64; complex ones stay complex
+        (fastmat casts both to float64, dropping imaginary parts)."""
+        v = getattr(self, '_largestSingularVectors', None)
+        if v is None:
+            if self.numRows > 1 and self.numCols > 1:
+                from scipy.sparse.linalg import svds
+                U, S, V = svds(self._promoted_operator(), 1,
+                               return_singular_vectors=True)
+            else:
+                U, S, V = np.linalg.svd(np.atleast_2d(self.array))
+            self._largestSingularValue = float(np.asarray(S)[0])
+            v = (U.astype(np.float64) if not np.iscomplexobj(U) else U,
+                 V.astype(np.float64) if not np.iscomplexobj(V) else V)
+            self._largestSingularVectors = v
+        return v
+
+    def _promoted_operator(self):
+        from scipy.sparse.linalg import LinearOperator
+        return LinearOperator(shape=self.shape, matvec=self.forward,
+                              rmatvec=self.backward, matmat=self.forward,
+                              dtype=np.promote_types(np.float64, self.dtype))
+
+    @property
+    def gram(self):
+        """A^H A as a fastmat operator (fastmat/Matrix.pyx:1026-1028)."""
+        g = getattr(self, '_gram', None)
+        if g is None:
+            from .operators import Product
+            g = self._gram = Product(self.H, self)
+        return g
+
+    @property
+    def inverse(self):
+        """The inverse, applied by an iterative solver
+        (fastmat/Matrix.pyx:1290-1291)."""
+        inv = getattr(self, '_inverse', None)
+        if inv is None:
+            inv = self._inverse = Inverse(self)
+        return inv
+
+    @property
+    def pseudoInverse(self):
+        """The Moore-Penrose pseudo-inverse, applied by least squares
+        (fastmat/Matrix.pyx:1313-1314)."""
+        inv = getattr(self, '_pseudoInverse', None)
+        if inv is None:
+            inv = self._pseudoInverse = PseudoInverse(self)
+        return inv
+
     # ------------------------------------------------------------ dense
     def reference(self):
         """Dense ground truth built without the fast transforms."""
@@ -418,24 +512,351 @@ class Matrix:
             return self._array.copy()
         raise NotImplementedError
 
+    #: bytes of unit vectors plus results per engine call when columns or
+    #: rows of the operator are formed on the GPU
+    _UNIT_BLOCK_BYTES = 1 << 28
+
+    def _unit_blocks(self, idx, direction, in_dtype):
+        """Yield (start, stop, Y) for consecutive blocks of the indices idx,
+        Y a CUDA tensor (n_out, stop - start) holding A e_i (forward) or
+        A^H e_i (backward) for i in idx[start:stop].  The unit vectors of a
+        block are written on the device and the whole block is one engine
+        call (as many columns as fit _UNIT_BLOCK_BYTES)."""
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("fastmat_gb300 needs a CUDA device")
+        n_in = self.numCols if direction == _native.FORWARD else self.numRows
+        n_out = self.numRows if direction == _native.FORWARD else self.numCols
+        in_dtype = np.dtype(in_dtype)
+        out_dtype = np.dtype(self._output_dtype(in_dtype))
+        per_col = n_in * in_dtype.itemsize + n_out * out_dtype.itemsize
+        k = int(max(1, min(len(idx), self._UNIT_BLOCK_BYTES // per_col)))
+        tdt = _torch_dtype(in_dtype)
+        idx_dev = torch.as_tensor(np.asarray(idx, dtype=np.int64),
+                                  device='cuda')
+        for a in range(0, len(idx), k):
+            b = min(a + k, len(idx))
+            e = torch.zeros((b - a, n_in), dtype=tdt, device='cuda')
+            e[torch.arange(b - a, device='cuda'), idx_dev[a:b]] = 1
+            yield a, b, self._transform_device(e.t(), direction)
+
+    def _unit_matrix(self, idx, direction, in_dtype):
+        """numpy (n_out, len(idx)) Fortran array of A e_i / A^H e_i."""
+        n_out = self.numRows if direction == _native.FORWARD else self.numCols
+        out = np.empty((n_out, len(idx)),
+                       dtype=self._output_dtype(np.dtype(in_dtype)),
+                       order='F')
+        for a, b, y in self._unit_blocks(idx, direction, in_dtype):
+            out[:, a:b] = y.t().cpu().numpy().T
+        return out
+
+    def _check_index(self, idx, size, what):
+        arr = np.asarray(idx)
+        if arr.size and (arr.min() < 0 or arr.max() >= size):
+            raise IndexError("%s index exceeds matrix dimensions." % what)
+
     @property
     def array(self):
-        """Dense array of the operator, computed with the fast transform
-        (forward applied to identity columns on the GPU)."""
+        """Dense array of the operator (fastmat/Matrix.pyx:360-387),
+        computed with the fast transform: the forward applied to identity
+        columns on the GPU, a block of columns per engine call.  Cached."""
         if self._array is not None:
             return self._array
-        eye = np.eye(self.numCols, dtype=np.int8)
-        return self.forward(eye)
+        a = getattr(self, '_arrayCache', None)
+        if a is None:
+            a = self.getArray()
+        return a
+
+    def getArray(self):
+        if self._array is not None:
+            return self._array
+        self._arrayCache = self._unit_matrix(
+            np.arange(self.numCols), _native.FORWARD, self.numpyType)
+        return self._arrayCache
+
+    def _dense_if_known(self):
+        return (self._array if self._array is not None
+                else getattr(self, '_arrayCache', None))
 
     def getCol(self, idx):
-        e = np.zeros(self.numCols, dtype=np.int8)
-        e[idx] = 1
-        return self.forward(e)
+        """Column idx (fastmat/Matrix.pyx:429-458)."""
+        if not np.isscalar(idx):
+            raise TypeError("Scalar index required.")
+        if idx < 0 or idx >= self.numCols:
+            raise IndexError("Column index exceeds matrix dimensions.")
+        d = self._dense_if_known()
+        if d is not None:
+            return np.squeeze(d[:, idx])
+        return self._getCol(idx)
+
+    def _getCol(self, idx):
+        return self._unit_matrix([idx], _native.FORWARD,
+                                 self.numpyType)[:, 0]
 
     def getRow(self, idx):
-        e = np.zeros(self.numRows, dtype=np.int8)
-        e[idx] = 1
-        return np.conj(self.backward(e))
+        """Row idx (fastmat/Matrix.pyx:501-530): the conjugate of A^H e_idx."""
+        if not np.isscalar(idx):
+            raise TypeError("Scalar index required.")
+        if idx < 0 or idx >= self.numRows:
+            raise IndexError("Row index exceeds matrix dimensions.")
+        d = self._dense_if_known()
+        if d is not None:
+            return np.squeeze(d[idx, :])
+        return self._getRow(idx)
+
+    def _getRow(self, idx):
+        return np.conj(self._unit_matrix([idx], _native.BACKWARD,
+                                         self.numpyType)[:, 0])
+
+    def _selection(self, indices, size):
+        if isinstance(indices, slice):
+            return np.arange(*indices.indices(size))
+        arr = np.array(indices)
+        if arr.ndim > 1:
+            raise IndexError("Index array must have at most one dimension.")
+        return arr.astype(np.int64)
+
+    def getCols(self, indices):
+        """Columns by index, slice or index vector
+        (fastmat/Matrix.pyx:389-427); all selected columns are formed by
+        one engine call per block of columns."""
+        if np.isscalar(indices):
+            return self.getCol(indices)
+        d = self._dense_if_known()
+        if d is not None:
+            return d[:, indices]
+        idx = self._selection(indices, self.numCols)
+        self._check_index(idx, self.numCols, "Column")
+        out = self._unit_matrix(idx, _native.FORWARD, self.numpyType)
+        return out.astype(self.numpyType, copy=False)
+
+    def getRows(self, indices):
+        """Rows by index, slice or index vector
+        (fastmat/Matrix.pyx:460-499)."""
+        if np.isscalar(indices):
+            return self.getRow(indices)
+        d = self._dense_if_known()
+        if d is not None:
+            return d[indices, :]
+        idx = self._selection(indices, self.numRows)
+        self._check_index(idx, self.numRows, "Row")
+        out = np.conj(self._unit_matrix(idx, _native.BACKWARD,
+                                        self.numpyType)).T
+        return np.ascontiguousarray(out).astype(self.numpyType, copy=False)
+
+    def _getItem(self, idxRow, idxCol):
+        d = self._dense_if_known()
+        if d is not None:
+            return d[idxRow, idxCol]
+        if self.numRows < self.numCols:
+            return self._getCol(idxCol)[idxRow]
+        return self._getRow(idxRow)[idxCol]
+
+    def __getitem__(self, tplIdx):
+        """Element, row, column or sub-array access
+        (fastmat/Matrix.pyx:532-658)."""
+        def selector(index, size):
+            if isinstance(index, (list, tuple, np.ndarray)):
+                arr = np.squeeze(np.asarray(index))
+                if arr.ndim == 0:
+                    arr = arr.reshape(1)
+                if not np.issubdtype(arr.dtype, np.integer):
+                    raise TypeError("Group indexing only allows int vectors.")
+                if arr.ndim != 1:
+                    raise IndexError("Group indexing vector must be 1D.")
+                return (arr[0] if arr.size == 1 else arr), arr.size
+            if index is Ellipsis:
+                return Ellipsis, size
+            if isinstance(index, slice):
+                slc = slice(*index.indices(size))
+                if slc.start == 0 and slc.stop == size and slc.step == 1:
+                    return Ellipsis, size
+                return slc, len(range(slc.start, slc.stop, slc.step))
+            if np.isscalar(index):
+                return index, 1
+            raise TypeError("Axis index is neither iterable, slice or int.")
+
+        rowSel, colSel = Ellipsis, Ellipsis
+        rowCount, colCount = self.numRows, self.numCols
+        if tplIdx is not Ellipsis:
+            if not isinstance(tplIdx, tuple):
+                raise IndexError("Invalid type of indexing tuple.")
+            if len(tplIdx) < 1 or len(tplIdx) > 2:
+                raise IndexError("None or too many indices given.")
+            rowSel, rowCount = selector(tplIdx[0], self.numRows)
+            if len(tplIdx) > 1:
+                colSel, colCount = selector(tplIdx[1], self.numCols)
+        if np.isscalar(rowSel):
+            if np.isscalar(colSel):
+                return self._getItem(rowSel, colSel)
+            return self._getRow(rowSel)[colSel]
+        if np.isscalar(colSel):
+            return self._getCol(colSel)[rowSel]
+        if rowSel is Ellipsis:
+            if colSel is Ellipsis:
+                return self.array
+            return self.getCols(colSel)
+        if colSel is Ellipsis:
+            return self.getRows(rowSel)
+        if rowCount <= 0 or colCount <= 0:
+            return None
+        if rowCount < colCount:
+            return self.getRows(rowSel)[:, colSel]
+        return self.getCols(colSel)[rowSel]
+
+    # ------------------------------------------------------------ norms
+    def _unit_norms(self, direction, size):
+        """Euclidean norms of A e_i (forward) or A^H e_i (backward) for every
+        i < size, float64, reduced on the GPU block by block (only the norms
+        come back to the host)."""
+        torch = _torch()
+        out = np.empty(size, dtype=np.float64)
+        for a, b, y in self._unit_blocks(np.arange(size), direction,
+                                          np.float64):
+            out[a:b] = torch.linalg.vector_norm(
+                y, dim=0).to(torch.float64).cpu().numpy()
+        return out
+
+    def _getColNorms(self):
+        return self._unit_norms(_native.FORWARD, self.numCols)
+
+    def _getRowNorms(self):
+        return self._unit_norms(_native.BACKWARD, self.numRows)
+
+    def _getColNormalized(self):
+        norms = self.colNorms
+        if np.any(norms == 0):
+            raise ValueError("Normalization: Matrix has zero-norm column.")
+        from .operators import Diag
+        return self * Diag(1. / norms)
+
+    def _getRowNormalized(self):
+        norms = self.rowNorms
+        if np.any(norms == 0):
+            raise ValueError("Normalization: Matrix has zero-norm row.")
+        from .operators import Diag
+        return Diag(1. / norms) * self
+
+    @property
+    def colNorms(self):
+        """Column norms, float64 (fastmat/Matrix.pyx:1035-1088).  Cached."""
+        v = getattr(self, '_colNorms', None)
+        if v is None:
+            v = self._colNorms = self._getColNorms()
+        return v
+
+    def getColNorms(self):
+        self._colNorms = self._getColNorms()
+        return self._colNorms
+
+    @property
+    def rowNorms(self):
+        """Row norms, float64 (fastmat/Matrix.pyx:1095-1148).  Cached."""
+        v = getattr(self, '_rowNorms', None)
+        if v is None:
+            v = self._rowNorms = self._getRowNorms()
+        return v
+
+    def getRowNorms(self):
+        self._rowNorms = self._getRowNorms()
+        return self._rowNorms
+
+    @property
+    def colNormalized(self):
+        """A diag(1 / colNorms) (fastmat/Matrix.pyx:1168-1177)."""
+        v = getattr(self, '_colNormalized', None)
+        if v is None:
+            v = self._colNormalized = self._getColNormalized()
+        return v
+
+    @property
+    def rowNormalized(self):
+        """diag(1 / rowNorms) A (fastmat/Matrix.pyx:1197-1206)."""
+        v = getattr(self, '_rowNormalized', None)
+        if v is None:
+            v = self._rowNormalized = self._getRowNormalized()
+        return v
+
+
+class _Solved(Matrix):
+    """An operator applied by solving with another: each column of the
+    input is one call of a scipy iterative solver whose matvecs are the
+    nested operator's GPU transforms (fastmat/Matrix.pyx:2490-2600)."""
+
+    def __init__(self, matrix, rows, cols, solver):
+        if not isinstance(matrix, Matrix):
+            raise TypeError("Inverse: Not a fastmat Matrix")
+        self._nested = matrix
+        self._content = (matrix, )
+        self._init_properties(rows, cols,
+                              np.promote_types(matrix.dtype, np.float32),
+                              **matrix._getProperties())
+        self._solver = solver
+
+    def _emit(self, b):
+        raise NotImplementedError(
+            "%s is applied by an iterative solver and cannot be fused into "
+            "a GPU plan" % self.__class__.__name__)
+
+    def _operator(self, direction):
+        op = self._nested.scipyLinearOperator
+        return op if direction == _native.FORWARD else op.H
+
+    def _transform(self, x, direction):
+        if _is_tensor(x):
+            x = x.cpu().numpy()
+        x = np.asarray(x)
+        if x.ndim < 1 or x.ndim > 2:
+            raise ValueError("Input data array must be 1D or 2D")
+        n_req = self.numCols if direction == _native.FORWARD else self.numRows
+        if x.shape[0] != n_req:
+            raise ValueError(
+                "Mismatch of vector size %d to relevant matrix axis %d" % (
+                    x.shape[0], n_req))
+        op = self._operator(direction)
+        flat = x.ndim == 1
+        x2 = x.reshape(n_req, 1) if flat else x
+        cols = [self._solver(op, x2[:, m], atol=1e-12)[0]
+                for m in range(x2.shape[1])]
+        n_out = self.numRows if direction == _native.FORWARD else self.numCols
+        y = (np.asfortranarray(np.stack(cols, axis=1)) if cols else
+             np.empty((n_out, 0), dtype=self.dtype, order='F'))
+        return y.reshape(n_out) if flat else y
+
+
+class Inverse(_Solved):
+    """A^-1 of a square operator, applied by scipy's lgmres
+    (fastmat/Matrix.pyx:2490-2541)."""
+
+    def __init__(self, matrix):
+        from scipy.sparse.linalg import lgmres
+        if not isinstance(matrix, Matrix):
+            raise TypeError("Inverse: Not a fastmat Matrix")
+        if matrix.shape[0] != matrix.shape[1]:
+            raise ValueError("Inverse: Matrix not square, so not invertible.")
+        super().__init__(matrix, matrix.shape[0], matrix.shape[0], lgmres)
+
+    def __repr__(self):
+        return "<%s.(^-1)>" % self._nested.__repr__()
+
+    def _reference(self):
+        return np.linalg.inv(self._nested.reference())
+
+
+class PseudoInverse(_Solved):
+    """A^+ applied by scipy's lsqr (fastmat/Matrix.pyx:2544-2600)."""
+
+    def __init__(self, matrix):
+        from scipy.sparse.linalg import lsqr
+        if not isinstance(matrix, Matrix):
+            raise TypeError("Inverse: Not a fastmat Matrix")
+        super().__init__(matrix, matrix.shape[1], matrix.shape[0], lsqr)
+
+    def __repr__(self):
+        return "<%s.(^+)>" % self._nested.__repr__()
+
+    def _reference(self):
+        return np.linalg.pinv(self._nested.reference())
 
 
 def _fcontig_tensor(t):

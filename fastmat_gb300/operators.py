@@ -84,6 +84,19 @@ class Diag(Matrix):
     def _reference(self):
         return np.diag(self._vecD)
 
+    # closed forms (fastmat/Diag.pyx:126-139)
+    def _getColNorms(self):
+        return np.abs(self._vecD)
+
+    _getRowNorms = _getColNorms
+
+    def _getColNormalized(self):
+        if np.iscomplexobj(self._vecD):
+            return Diag((self._vecD / np.abs(self._vecD)).astype(self.dtype))
+        return Diag(np.sign(self._vecD).astype(self.dtype))
+
+    _getRowNormalized = _getColNormalized
+
 
 class Eye(Matrix):
     """Identity (fastmat/Eye.pyx)."""
@@ -96,6 +109,17 @@ class Eye(Matrix):
 
     def _reference(self):
         return np.eye(self.numRows, dtype=self.dtype)
+
+    # closed forms (fastmat/Eye.pyx:92-102)
+    def _getColNorms(self):
+        return np.ones((self.numCols, ), dtype=self.dtype)
+
+    _getRowNorms = _getColNorms
+
+    def _getColNormalized(self):
+        return self
+
+    _getRowNormalized = _getColNormalized
 
 
 class Hadamard(Matrix):
@@ -157,6 +181,17 @@ class Permutation(Matrix):
 
     def _reference(self):
         return np.eye(self.numRows, dtype=self.dtype)[self._sigma, :]
+
+    # closed forms (fastmat/Permutation.pyx:104-114)
+    def _getColNorms(self):
+        return np.ones((self.numCols, ), dtype=self.dtype)
+
+    _getRowNorms = _getColNorms
+
+    def _getColNormalized(self):
+        return self
+
+    _getRowNormalized = _getColNormalized
 
 
 class Partial(Matrix):

@@ -3,7 +3,8 @@
 Run in a container where the reference is built (``oracle/build_reference.sh``
 builds it into ``baseline/_ref/src``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py               # everything
+    python tests/golden/make_golden.py --accessors   # accessors.npz only
 
 Each case is an operator expression over named parameter arrays, written in
 the class vocabulary that fastmat, the oracle and ``fastmat_gb300`` share
@@ -224,5 +225,61 @@ def main():
     print('wrote %d operator cases' % len(meta))
 
 
+def accessors():
+    """The reference's dense accessors on the small cases with a dense
+    reference (fastmat/Matrix.pyx:360-658 and 1035-1206): ``array``,
+    ``getCols`` / ``getRows`` of a few indices, elements ``A[i, j]``,
+    ``colNorms`` / ``rowNorms`` and (up to 64 x 64) the normalized
+    operators' arrays, written to accessors.npz.  The operators are rebuilt from the
+    parameters stored in operators.npz."""
+    ns = namespace()
+    data = np.load(os.path.join(HERE, 'operators.npz'))
+    with open(os.path.join(HERE, 'operators.json')) as f:
+        meta = json.load(f)
+    rec = {}
+    names = []
+    for m in meta:
+        if not m['dense']:
+            continue
+        name = m['name']
+        env = dict(ns)
+        env.update({k: data['%s__p_%s' % (name, k)] for k in m['params']})
+        op = eval(m['expr'], env)  # noqa: S307 (fixture expressions)
+        n_rows, n_cols = op.shape
+        cols = np.unique(np.array([0, n_cols // 2, n_cols - 1]))
+        rows = np.unique(np.array([0, n_rows // 3, n_rows - 1]))
+        got = {}
+        for key, fn in (
+                ('array', lambda: op.array),
+                ('cols', lambda: op.getCols(cols)),
+                ('rows', lambda: op.getRows(rows)),
+                ('items', lambda: np.array([op[int(i), int(j)]
+                                            for i in rows for j in cols])),
+                ('colnorms', lambda: op.colNorms),
+                ('rownorms', lambda: op.rowNorms),
+                ('colnormalized', lambda: op.colNormalized.array),
+                ('rownormalized', lambda: op.rowNormalized.array)):
+            try:
+                got[key] = np.asarray(fn())
+            except Exception as e:  # noqa: BLE001 (recorded as absent)
+                print('%s.%s: reference raised %s' % (name, key,
+                                                      type(e).__name__))
+        if n_rows * n_cols > 64 * 64:
+            # the normalized arrays only for the smaller operators
+            got.pop('colnormalized', None)
+            got.pop('rownormalized', None)
+        for key, v in got.items():
+            rec['%s__%s' % (name, key)] = v
+        rec['%s__colidx' % name] = cols
+        rec['%s__rowidx' % name] = rows
+        names.append(name)
+    np.savez_compressed(os.path.join(HERE, 'accessors.npz'), **rec)
+    print('wrote accessors for %d cases' % len(names))
+
+
 if __name__ == '__main__':
-    main()
+    if sys.argv[1:] == ['--accessors']:
+        accessors()
+    else:
+        main()
+        accessors()

@@ -40,6 +40,17 @@ def load_cases():
     return [Case(m, data) for m in meta]
 
 
+def load_accessors():
+    """name -> {key: array} of the reference's dense accessors
+    (tests/golden/accessors.npz)."""
+    data = np.load(os.path.join(HERE, 'accessors.npz'))
+    out = {}
+    for k in data.files:
+        name, key = k.split('__')
+        out.setdefault(name, {})[key] = data[k]
+    return out
+
+
 def load_fftsizes():
     return np.load(os.path.join(HERE, 'fftsizes.npz'))
 

@@ -5,8 +5,8 @@ import numpy as np
 import pytest
 
 from oracle import fm_oracle as fo
-from tests.golden_cases import (load_cases, load_circulant1024,
-                                load_fftsizes, tolerance)
+from tests.golden_cases import (load_accessors, load_cases,
+                                load_circulant1024, load_fftsizes, tolerance)
 
 CASES = load_cases()
 
@@ -40,6 +40,37 @@ def test_oracle_matches_reference(case):
     if case.dense is not None:
         d = op.dense()
         assert fo.rel_err(d, case.dense) <= 1e-12
+
+
+ACC = load_accessors()
+
+
+@pytest.mark.parametrize('case', [c for c in CASES if c.name in ACC],
+                         ids=lambda c: c.name)
+def test_oracle_pins_accessor_fixtures(case):
+    """The reference's array / getCols / getRows / elements / norms agree
+    with the oracle's dense matrix."""
+    acc = ACC[case.name]
+    d = case.build(NS).dense()
+    scale = max(1e-300, float(np.max(np.abs(d))))
+
+    def close(a, b):
+        return float(np.max(np.abs(np.asarray(a) - np.asarray(b)),
+                            initial=0.0)) / scale <= 1e-12
+
+    ci, ri = acc['colidx'], acc['rowidx']
+    assert close(acc['array'], d)
+    assert close(acc['cols'], d[:, ci])
+    assert close(acc['rows'], d[ri, :])
+    assert close(acc['items'], d[np.ix_(ri, ci)].reshape(-1))
+    assert np.allclose(acc['colnorms'], np.linalg.norm(d, axis=0),
+                       rtol=1e-12, atol=1e-12 * scale)
+    assert np.allclose(acc['rownorms'], np.linalg.norm(d, axis=1),
+                       rtol=1e-12, atol=1e-12 * scale)
+    if 'colnormalized' in acc:
+        assert close(acc['colnormalized'] * np.linalg.norm(d, axis=0), d)
+        assert close(acc['rownormalized'] *
+                     np.linalg.norm(d, axis=1)[:, None], d)
 
 
 def test_fft_size_heuristics_match_reference():
