@@ -7,8 +7,9 @@ Drop-in classes with fastmat's constructors and ``forward``/``backward``/
 
 from .matrix import (Conjugate, Hermitian, Inverse, Matrix, PseudoInverse,
                      Transpose)
-from .operators import (Circulant, Diag, Eye, Fourier, Hadamard, Kron,
-                        Partial, Permutation, Product, Sum, Toeplitz)
+from .operators import (BlockDiag, Blocks, Circulant, Diag, Eye, Fourier,
+                        Hadamard, Kron, Partial, Permutation, Product, Sum,
+                        Toeplitz)
 from . import _native
 from . import algorithms
 from .batch import Batch
@@ -18,7 +19,8 @@ __version__ = '0.1.0'
 
 __all__ = ['Matrix', 'Hermitian', 'Conjugate', 'Transpose', 'Fourier',
            'Circulant', 'Toeplitz', 'Hadamard', 'Diag', 'Eye', 'Partial',
-           'Permutation', 'Product', 'Sum', 'Kron', 'Inverse', 'PseudoInverse',
+           'Permutation', 'Product', 'Sum', 'Kron', 'Blocks', 'BlockDiag',
+           'Inverse', 'PseudoInverse',
            'Batch', 'build']
 
 

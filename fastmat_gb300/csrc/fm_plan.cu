@@ -199,6 +199,8 @@ int grid_for(i64 n) { return (int)std::min<i64>((n + 255) / 256, 4096); }
 struct LStep {
   fmk::Step st;
   int src, dst;  // 0 = x, 1 = y, >= 2 scratch
+  // first row of the launch's operand inside its buffer (Blocks segments)
+  i64 src_off = 0, dst_off = 0;
   int cls, threads;
   size_t smem;
   int lay = 0;                     // tile layout (1: element-major)
@@ -282,7 +284,7 @@ struct Unit;
 typedef std::vector<Unit> Chain;
 
 struct Unit {
-  enum Kind { PROG, STEPS, SUM } kind = PROG;
+  enum Kind { PROG, STEPS, SUM, BLOCKS } kind = PROG;
   i64 n_in = 0, n_out = 0;
   // PROG
   std::vector<fmk::Op> ops;
@@ -292,6 +294,11 @@ struct Unit {
   std::vector<i64> tmp_rows;
   // SUM
   std::vector<Chain> terms;
+  // BLOCKS: grid[o][q] maps input segment q to output segment o (has = 0:
+  // zero block); segment lengths in rows
+  std::vector<std::vector<Chain>> grid;
+  std::vector<std::vector<int>> has;
+  std::vector<i64> seg_in, seg_out;
 };
 
 struct NodeRec {
@@ -1156,6 +1163,56 @@ class Planner {
         return c;
       }
       case FM_NODE_KRON: return kron(r, fwd);
+      case FM_NODE_BLOCKS: {
+        const i64 R = d.n, k = (i64)r.ch.size();
+        if (R < 1 || k < 1 || k % R)
+          fail(FM_ERR_VALUE, "Blocks: children do not form a grid");
+        const i64 C = k / R;
+        std::vector<i64> hr((size_t)R, -1), wc((size_t)C, -1);
+        for (i64 i = 0; i < R; ++i)
+          for (i64 j = 0; j < C; ++j) {
+            const int ch = r.ch[(size_t)(i * C + j)];
+            if (ch < 0) continue;
+            const fm_node &b = nodes_[ch].d;
+            if ((hr[i] >= 0 && hr[i] != b.rows) ||
+                (wc[j] >= 0 && wc[j] != b.cols))
+              fail(FM_ERR_VALUE, "Blocks: block shapes do not form a grid");
+            hr[i] = b.rows;
+            wc[j] = b.cols;
+          }
+        i64 sr = 0, sc = 0;
+        for (i64 v : hr) {
+          if (v < 0) fail(FM_ERR_VALUE, "Blocks: a block row holds no block");
+          sr += v;
+        }
+        for (i64 v : wc) {
+          if (v < 0)
+            fail(FM_ERR_VALUE, "Blocks: a block column holds no block");
+          sc += v;
+        }
+        if (sr != d.rows || sc != d.cols)
+          fail(FM_ERR_VALUE, "Blocks: blocks do not add up to the shape");
+        Unit u;
+        u.kind = Unit::BLOCKS;
+        u.n_in = n_in;
+        u.n_out = n_out;
+        // forward: output segments are the block rows; the adjoint swaps
+        // rows and columns and takes every block's adjoint
+        u.seg_out = fwd ? hr : wc;
+        u.seg_in = fwd ? wc : hr;
+        u.grid.assign(u.seg_out.size(), std::vector<Chain>(u.seg_in.size()));
+        u.has.assign(u.seg_out.size(), std::vector<int>(u.seg_in.size(), 0));
+        for (i64 i = 0; i < R; ++i)
+          for (i64 j = 0; j < C; ++j) {
+            const int ch = r.ch[(size_t)(i * C + j)];
+            if (ch < 0) continue;
+            const size_t o = (size_t)(fwd ? i : j), q = (size_t)(fwd ? j : i);
+            u.grid[o][q] = compile(ch, fwd);
+            u.has[o][q] = 1;
+          }
+        c.push_back(u);
+        return c;
+      }
       case FM_NODE_HERMITIAN: return compile(r.ch.at(0), !fwd);
       case FM_NODE_CONJUGATE: {
         c.push_back(prog({mkop(fmk::OP_CONJ, (int)n_in)}, n_in, n_in, n_in));
@@ -1605,10 +1662,61 @@ class Planner {
           }
           break;
         }
+        case Unit::BLOCKS: {
+          // output segment o = sum over q of block (o, q) applied to input
+          // segment q: the first block writes, later ones go through
+          // scratch and accumulate
+          i64 oo = 0;
+          for (size_t o = 0; o < u.grid.size(); ++o) {
+            const i64 m = u.seg_out[o];
+            bool first = true;
+            i64 io = 0;
+            for (size_t q = 0; q < u.grid[o].size(); ++q) {
+              const i64 nq = u.seg_in[q];
+              if (u.has[o][q]) {
+                if (first) {
+                  lower_at(u.grid[o][q], cur, io, nq, dst, oo, m, out);
+                  first = false;
+                } else {
+                  const int tmp = new_scratch(m);
+                  lower_at(u.grid[o][q], cur, io, nq, tmp, 0, m, out);
+                  Unit cp = prog({}, m, m, m);
+                  std::vector<LStep> acc;
+                  emit_prog(cp, tmp, dst, acc);
+                  for (LStep &a : acc) {
+                    a.st.accumulate = 1;
+                    a.tma_out_ok = 0;
+                    a.dst_off += oo;
+                  }
+                  out.insert(out.end(), acc.begin(), acc.end());
+                }
+              }
+              io += nq;
+            }
+            oo += m;
+          }
+          break;
+        }
       }
       cur = dst;
     }
     (void)out_rows;
+  }
+
+  // lower a chain that reads rows [in_off, in_off + in_rows) of buffer in_id
+  // and writes rows [out_off, out_off + out_rows) of buffer out_id
+  void lower_at(const Chain &ch, int in_id, i64 in_off, i64 in_rows,
+                int out_id, i64 out_off, i64 out_rows,
+                std::vector<LStep> &out) {
+    std::vector<LStep> part;
+    lower(ch, in_id, in_rows, out_id, out_rows, part);
+    for (LStep &ls : part) {
+      if (ls.src == in_id) ls.src_off += in_off;
+      else if (ls.src == out_id) ls.src_off += out_off;
+      if (ls.dst == out_id) ls.dst_off += out_off;
+      else if (ls.dst == in_id) ls.dst_off += in_off;
+    }
+    out.insert(out.end(), part.begin(), part.end());
   }
 };
 
@@ -1783,8 +1891,8 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
     const void *dp;
     bind(ls.src, sp, st.src_type, st.ld_src);
     bind(ls.dst, dp, st.dst_type, st.ld_dst);
-    st.src = sp;
-    st.dst = const_cast<void *>(dp);
+    st.src = (const char *)sp + ls.src_off * esize(st.src_type);
+    st.dst = (char *)const_cast<void *>(dp) + ls.dst_off * esize(st.dst_type);
     st.num_cols = M;
     launch_step(P, ls, st, s);
     if (events) CUDA_TRY(cudaEventRecord((*events)[li++], s));
@@ -1859,8 +1967,8 @@ int run_plan_static(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
     const void *dp;
     bind(ls.src, sp, st.src_type, st.ld_src);
     bind(ls.dst, dp, st.dst_type, st.ld_dst);
-    st.src = sp;
-    st.dst = const_cast<void *>(dp);
+    st.src = (const char *)sp + ls.src_off * esize(st.src_type);
+    st.dst = (char *)const_cast<void *>(dp) + ls.dst_off * esize(st.dst_type);
     st.num_cols = M;
     launch_step(P, ls, st, s);
   }
@@ -1933,7 +2041,9 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
         fail(FM_ERR_VALUE, "invalid child range");
       for (int k = 0; k < d.num_children; ++k) {
         const int c = children[d.first_child + k];
-        if (c < 0 || c >= num_nodes) fail(FM_ERR_VALUE, "invalid child");
+        // -1 marks a zero block of a Blocks node
+        if (c < -1 || c >= num_nodes || (c == -1 && d.kind != FM_NODE_BLOCKS))
+          fail(FM_ERR_VALUE, "invalid child");
         recs[i].ch.push_back(c);
       }
       if (d.rows < 0 || d.cols < 0) fail(FM_ERR_VALUE, "negative shape");
@@ -2383,8 +2493,9 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
         const void *sp, *dp;
         bind(ls.src, sp, st.src_type, st.ld_src);
         bind(ls.dst, dp, st.dst_type, st.ld_dst);
-        st.src = sp;
-        st.dst = const_cast<void *>(dp);
+        st.src = (const char *)sp + ls.src_off * esize(st.src_type);
+        st.dst =
+            (char *)const_cast<void *>(dp) + ls.dst_off * esize(st.dst_type);
         st.num_cols = M;
         st.err = B->status + 1;
         st.tma_in = st.tma_out = 0;

@@ -50,7 +50,8 @@ class _Builder:
         node.vec1, node.len1, node.type1 = p, ln, t
         s = complex(scalar)
         node.scalar_re, node.scalar_im = s.real, s.imag
-        idx = [c._emit(self) for c in children]
+        # None: an empty (zero) block of a Blocks node
+        idx = [-1 if c is None else c._emit(self) for c in children]
         node.first_child = len(self.children)
         node.num_children = len(idx)
         self.children.extend(idx)

@@ -617,3 +617,100 @@ class Toeplitz(Partial):
         d = np.arange(nr)[:, None] - np.arange(nc)[None, :]
         full = np.concatenate([self.vecR, self.vecC])
         return full[d + nc - 1].astype(self.dtype)
+
+
+class Blocks(Matrix):
+    """A grid of operators (fastmat/Blocks.pyx:27-312): the inner iterables
+    are block rows; blocks of a row share their height, blocks of a column
+    their width.  One GPU plan: output block row r is the sum over c of
+    block (r, c) applied to input segment c (the first block writes, later
+    ones accumulate); the adjoint runs the transposed grid of adjoints."""
+
+    def __init__(self, arrMatrices, **options):
+        if not isinstance(arrMatrices, (list, tuple)):
+            raise ValueError("Blocks: Not a nested list of fastmat matrices.")
+        if len(arrMatrices) < 1:
+            raise ValueError("Blocks: Contains no matrices.")
+        for rr, row in enumerate(arrMatrices):
+            if isinstance(row, Matrix):
+                raise TypeError(
+                    "Blocks.row(%d) is of type %s. Instantiate Blocks with a "
+                    "2D structure of iterables (e.g. nested lists) holding "
+                    "fastmat Matrix instances in their second level." % (
+                        rr, repr(row)))
+            for cc, item in enumerate(row):
+                if not isinstance(item, Matrix):
+                    raise TypeError(
+                        "Blocks[%d, %d] is of type %s and not a fastmat "
+                        "Matrix isntance." % (rr, cc, repr(item)))
+        self._rows = tuple(tuple(r) for r in arrMatrices)
+        first = self._rows[0]
+        self._rowSize = tuple(r[0].numRows for r in self._rows)
+        self._colSize = tuple(t.numCols for t in first)
+        dtype = np.int8
+        for rr, row in enumerate(self._rows):
+            if len(row) != len(first):
+                raise ValueError(
+                    "Blocks.row(%d) has incompatible number of entries" % rr)
+            for cc, term in enumerate(row):
+                if term.numRows != row[0].numRows:
+                    raise ValueError(
+                        "Blocks[%d,%d] with shape %s is incompatible with row "
+                        "height (%d,:)" % (rr, cc, str(term.shape),
+                                           row[0].numRows))
+                if term.numCols != first[cc].numCols:
+                    raise ValueError(
+                        "Blocks[%d,%d] with shape %s is incompatible with "
+                        "column width (:,%d)" % (rr, cc, str(term.shape),
+                                                 first[cc].numCols))
+                dtype = np.promote_types(dtype, term.dtype)
+        self._cols = tuple(tuple(r[cc] for r in self._rows)
+                           for cc in range(len(first)))
+        self._content = tuple(t for r in self._rows for t in r)
+        self._init_properties(sum(self._rowSize), sum(self._colSize),
+                              dtype, **options)
+        self._widenInputDatatype = True
+
+    def _emit(self, b):
+        return b.add(_native.NODE_BLOCKS, self, children=self._content,
+                     n=len(self._rows))
+
+    def _reference(self):
+        return np.block([[t.reference() for t in r] for r in self._rows]
+                        ).astype(self.dtype)
+
+
+class BlockDiag(Matrix):
+    """Operators along the block diagonal (fastmat/BlockDiag.pyx:27-200),
+    planned as a Blocks grid whose off-diagonal blocks are zero: every
+    block reads and writes its own row segment, one GPU plan."""
+
+    def __init__(self, *matrices, **options):
+        if len(matrices) < 1:
+            raise ValueError("You must specify at least one matrix.")
+        dtype = np.int8
+        for term in matrices:
+            if not isinstance(term, Matrix):
+                raise ValueError(
+                    "Only fastmat matrices supported, %s given." % str(term))
+            dtype = np.promote_types(dtype, term.dtype)
+        self._content = tuple(matrices)
+        self._init_properties(sum(t.numRows for t in matrices),
+                              sum(t.numCols for t in matrices), dtype,
+                              **options)
+        self._widenInputDatatype = True
+
+    def _emit(self, b):
+        k = len(self._content)
+        grid = [self._content[i] if i == j else None
+                for i in range(k) for j in range(k)]
+        return b.add(_native.NODE_BLOCKS, self, children=grid, n=k)
+
+    def _reference(self):
+        out = np.zeros(self.shape, dtype=self.dtype)
+        r = c = 0
+        for t in self._content:
+            out[r:r + t.numRows, c:c + t.numCols] = t.reference()
+            r += t.numRows
+            c += t.numCols
+        return out

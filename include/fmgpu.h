@@ -81,6 +81,12 @@ extern "C" {
 #define FM_NODE_CONJUGATE 12   /* one child; conj o child o conj              */
 #define FM_NODE_EYE 13         /* identity of size rows                       */
 #define FM_NODE_DENSE 14       /* vec0 = rows x cols matrix, column-major     */
+#define FM_NODE_BLOCKS 15      /* n = number of block rows R; children = the
+                                  R x C blocks row by row, -1 for a zero
+                                  block (every block row and block column
+                                  holds at least one block); blocks of a row
+                                  share their height, of a column their
+                                  width (fastmat's Blocks and BlockDiag)     */
 
 typedef struct fm_node {
     int32_t kind;

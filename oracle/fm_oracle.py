@@ -445,6 +445,95 @@ class Sum(Op):
         return sum(t.dense().astype(np.complex128) for t in self.terms)
 
 
+class Blocks(Op):
+    """fastmat/Blocks.pyx:65-312: a grid of operators; output block row r
+    is the sum over c of block (r, c) applied to input segment c."""
+
+    def __init__(self, rows):
+        self.rows = [list(r) for r in rows]
+        self.heights = [r[0].shape[0] for r in self.rows]
+        self.widths = [t.shape[1] for t in self.rows[0]]
+        for r in self.rows:
+            if len(r) != len(self.widths):
+                raise ValueError("Blocks: incompatible number of entries")
+            for c, t in enumerate(r):
+                if t.shape != (r[0].shape[0], self.widths[c]):
+                    raise ValueError("Blocks: block shapes do not match")
+        dtype = np.int8
+        for r in self.rows:
+            for t in r:
+                dtype = promote(dtype, t.dtype)
+        self.dtype = dtype
+        self.shape = (sum(self.heights), sum(self.widths))
+        self.widen_input = True
+
+    @staticmethod
+    def _cuts(sizes):
+        return np.concatenate([[0], np.cumsum(sizes)]).astype(int)
+
+    def _fwd(self, x):
+        ro, ci = self._cuts(self.heights), self._cuts(self.widths)
+        y = np.zeros((self.shape[0], x.shape[1]), self.out_dtype(x.dtype))
+        for r, row in enumerate(self.rows):
+            for c, t in enumerate(row):
+                y[ro[r]:ro[r + 1]] += t.forward(x[ci[c]:ci[c + 1]])
+        return y
+
+    def _bwd(self, x):
+        ro, ci = self._cuts(self.heights), self._cuts(self.widths)
+        y = np.zeros((self.shape[1], x.shape[1]), self.out_dtype(x.dtype))
+        for r, row in enumerate(self.rows):
+            for c, t in enumerate(row):
+                y[ci[c]:ci[c + 1]] += t.backward(x[ro[r]:ro[r + 1]])
+        return y
+
+    def dense(self):
+        return np.block([[t.dense().astype(np.complex128) for t in r]
+                         for r in self.rows])
+
+
+class BlockDiag(Op):
+    """fastmat/BlockDiag.pyx:95-200: operators along the block diagonal."""
+
+    def __init__(self, *terms):
+        if len(terms) < 1:
+            raise ValueError("You must specify at least one matrix.")
+        self.terms = terms
+        dtype = np.int8
+        for t in terms:
+            dtype = promote(dtype, t.dtype)
+        self.dtype = dtype
+        self.shape = (sum(t.shape[0] for t in terms),
+                      sum(t.shape[1] for t in terms))
+        self.widen_input = True
+
+    def _apply(self, x, fwd):
+        n_out = self.shape[0] if fwd else self.shape[1]
+        y = np.zeros((n_out, x.shape[1]), self.out_dtype(x.dtype))
+        i = o = 0
+        for t in self.terms:
+            n_i, n_o = (t.shape[1], t.shape[0]) if fwd else t.shape
+            y[o:o + n_o] = (t.forward if fwd else t.backward)(x[i:i + n_i])
+            i += n_i
+            o += n_o
+        return y
+
+    def _fwd(self, x):
+        return self._apply(x, True)
+
+    def _bwd(self, x):
+        return self._apply(x, False)
+
+    def dense(self):
+        a = np.zeros(self.shape, np.complex128)
+        r = c = 0
+        for t in self.terms:
+            a[r:r + t.shape[0], c:c + t.shape[1]] = t.dense()
+            r += t.shape[0]
+            c += t.shape[1]
+        return a
+
+
 class Kron(Op):
     """fastmat/Kron.pyx:79-353: mode-wise application, np.kron ordering
     (factor 0 is the most significant index)."""

@@ -38,7 +38,8 @@ def namespace():
         Hadamard=fm.Hadamard, Kron=fm.Kron, Diag=fm.Diag, Partial=fm.Partial,
         Permutation=fm.Permutation, Product=fm.Product, Sum=fm.Sum,
         Hermitian=fm.Hermitian, Conjugate=fm.Conjugate,
-        Transpose=fm.Transpose, Eye=fm.Eye, Matrix=fm.Matrix, np=np)
+        Transpose=fm.Transpose, Eye=fm.Eye, Matrix=fm.Matrix,
+        Blocks=fm.Blocks, BlockDiag=fm.BlockDiag, np=np)
 
 
 def cases():
@@ -155,6 +156,38 @@ def cases():
     add('toeplitz_ml_rect', 'Toeplitz(tm, split=sp)',
         {'tm': cplx(rng, 4, 3), 'sp': np.array([4, 1])})
     add('toeplitz_ml_9x7', 'Toeplitz(tm)', {'tm': cplx(rng, 9, 7)})
+    # block compositions (fastmat/Blocks.pyx, fastmat/BlockDiag.pyx)
+    add('blockdiag_mixed',
+        'BlockDiag(Circulant(c), Fourier(5), Diag(d), Hadamard(2))',
+        {'c': cplx(rng, 7), 'd': cplx(rng, 4)})
+    add('blockdiag_real', 'BlockDiag(Hadamard(3), Diag(d))',
+        {'d': rng.standard_normal(5)}, xdtype=np.float64)
+    add('blockdiag_one', 'BlockDiag(Toeplitz(tc, tr))',
+        {'tc': cplx(rng, 6), 'tr': cplx(rng, 4)})
+    add('blocks_2x3',
+        'Blocks([[Circulant(c1), Partial(Fourier(9), rows=r6, cols=k9), '
+        'Partial(Hadamard(3), rows=r6b, cols=k4)], '
+        '[Partial(Circulant(c2), rows=r4, cols=k6), '
+        'Partial(Fourier(9), rows=r4b, cols=k9), Diag(d4)]])',
+        {'c1': cplx(rng, 6), 'c2': cplx(rng, 6), 'd4': cplx(rng, 4),
+         'r6': np.sort(rng.choice(9, 6, replace=False)),
+         'r6b': np.sort(rng.choice(8, 6, replace=False)),
+         'k4': np.sort(rng.choice(8, 4, replace=False)),
+         'r4': np.sort(rng.choice(6, 4, replace=False)),
+         'r4b': np.sort(rng.choice(9, 4, replace=False)),
+         'k6': np.arange(6), 'k9': np.arange(9)})
+    add('blocks_nested',
+        'Blocks([[Product(Fourier(4), Diag(d4)), '
+        'Kron(Hadamard(1), Circulant(c2))], '
+        '[Eye(4), BlockDiag(Fourier(3), Diag(d1))]])',
+        {'d4': cplx(rng, 4), 'c2': cplx(rng, 2), 'd1': cplx(rng, 1)})
+    add('blocks_real', 'Blocks([[Hadamard(2), Diag(d)], [Diag(e), Eye(4)]])',
+        {'d': rng.standard_normal(4), 'e': rng.standard_normal(4)},
+        xdtype=np.float64)
+    add('blocks_large', 'Blocks([[Circulant(c), Fourier(300)], '
+        '[Toeplitz(tc, tr), Diag(d)]])',
+        {'c': cplx(rng, 300), 'tc': cplx(rng, 300), 'tr': cplx(rng, 299),
+         'd': cplx(rng, 300)}, dense=False)
     return out
 
 

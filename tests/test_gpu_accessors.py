@@ -24,7 +24,8 @@ def _ns():
                 Diag=fg.Diag, Partial=fg.Partial,
                 Permutation=fg.Permutation, Product=fg.Product, Sum=fg.Sum,
                 Hermitian=fg.Hermitian, Conjugate=fg.Conjugate,
-                Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix, np=np)
+                Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix,
+                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
 
 
 def _tol(ref):

@@ -20,7 +20,8 @@ def _ns():
                 Diag=fg.Diag, Partial=fg.Partial,
                 Permutation=fg.Permutation, Product=fg.Product, Sum=fg.Sum,
                 Hermitian=fg.Hermitian, Conjugate=fg.Conjugate,
-                Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix, np=np)
+                Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix,
+                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
 
 
 ONS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
@@ -28,7 +29,7 @@ ONS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
            Partial=fo.Partial, Permutation=fo.Permutation,
            Product=fo.Product, Sum=fo.Sum, Hermitian=fo.Hermitian,
            Conjugate=fo.Conjugate, Transpose=fo.Transpose, Eye=fo.Eye,
-           Matrix=fo.Dense, np=np)
+           Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag, np=np)
 
 
 def _close(out, ref, x, name=None):

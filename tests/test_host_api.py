@@ -21,7 +21,7 @@ NS = dict(Fourier=fg.Fourier, Circulant=fg.Circulant, Toeplitz=fg.Toeplitz,
           Partial=fg.Partial, Permutation=fg.Permutation,
           Product=fg.Product, Sum=fg.Sum, Hermitian=fg.Hermitian,
           Conjugate=fg.Conjugate, Transpose=fg.Transpose, Eye=fg.Eye,
-          Matrix=fg.Matrix, np=np)
+          Matrix=fg.Matrix, Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
 
 
 @pytest.mark.parametrize('case', CASES, ids=lambda c: c.name)
@@ -138,3 +138,32 @@ def test_node_struct_layout_matches_header(tmp_path):
                     _native.FmNode.scalar_im.offset,
                     ctypes.sizeof(_native.FmPlanInfo),
                     _native.FmPlanInfo.compute_type.offset]
+
+
+def test_block_constructors_validate_like_fastmat():
+    """fastmat/Blocks.pyx:65-196 and fastmat/BlockDiag.pyx:95-130."""
+    F4, H2, F3 = fg.Fourier(4), fg.Hadamard(2), fg.Fourier(3)
+    with pytest.raises(ValueError):
+        fg.Blocks(F4)
+    with pytest.raises(ValueError):
+        fg.Blocks([])
+    with pytest.raises(TypeError):
+        fg.Blocks([F4, H2])
+    with pytest.raises(TypeError):
+        fg.Blocks([[F4, np.eye(4)]])
+    with pytest.raises(ValueError):
+        fg.Blocks([[F4, H2], [H2]])
+    with pytest.raises(ValueError):
+        fg.Blocks([[F4, F3]])
+    with pytest.raises(ValueError):
+        fg.Blocks([[F4], [fg.Partial(F3, rows=np.arange(2))]])
+    with pytest.raises(ValueError):
+        fg.BlockDiag()
+    with pytest.raises(ValueError):
+        fg.BlockDiag(F4, np.eye(3))
+    B = fg.Blocks([[F4, H2], [fg.Diag(np.ones(4)), fg.Eye(4)]])
+    assert B.shape == (8, 8) and B.dtype == np.complex128
+    assert len(B.content) == 4
+    D = fg.BlockDiag(F3, H2, fg.Diag(np.arange(2.0)))
+    assert D.shape == (9, 9) and D.dtype == np.complex128
+    assert fg.BlockDiag(H2, fg.Eye(2)).dtype == np.int8

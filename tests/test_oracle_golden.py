@@ -15,7 +15,7 @@ NS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
           Partial=fo.Partial, Permutation=fo.Permutation,
           Product=fo.Product, Sum=fo.Sum, Hermitian=fo.Hermitian,
           Conjugate=fo.Conjugate, Transpose=fo.Transpose, Eye=fo.Eye,
-          Matrix=fo.Dense, np=np)
+          Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag, np=np)
 
 
 def expected_dtype(op_dtype, x_dtype):
