@@ -8,8 +8,8 @@ Drop-in classes with fastmat's constructors and ``forward``/``backward``/
 from .matrix import (Conjugate, Hermitian, Inverse, Matrix, PseudoInverse,
                      Transpose)
 from .operators import (BlockDiag, Blocks, Circulant, Diag, Eye, Fourier,
-                        Hadamard, Kron, Partial, Permutation, Product, Sum,
-                        Toeplitz)
+                        Hadamard, Kron, Partial, Permutation, Product,
+                        Sparse, Sum, Toeplitz)
 from . import _native
 from . import algorithms
 from .batch import Batch
@@ -20,6 +20,7 @@ __version__ = '0.1.0'
 __all__ = ['Matrix', 'Hermitian', 'Conjugate', 'Transpose', 'Fourier',
            'Circulant', 'Toeplitz', 'Hadamard', 'Diag', 'Eye', 'Partial',
            'Permutation', 'Product', 'Sum', 'Kron', 'Blocks', 'BlockDiag',
+           'Sparse',
            'Inverse', 'PseudoInverse',
            'Batch', 'build']
 

@@ -39,7 +39,7 @@ FM_F32_TC = 18   # float32, Hadamard 16-point groups on the tensor cores
 (NODE_FOURIER, NODE_CIRCULANT, NODE_TOEPLITZ, NODE_HADAMARD, NODE_DIAG,
  NODE_PARTIAL, NODE_PERMUTATION, NODE_PRODUCT, NODE_SUM, NODE_KRON,
  NODE_HERMITIAN, NODE_CONJUGATE, NODE_EYE, NODE_DENSE,
- NODE_BLOCKS) = range(1, 16)
+ NODE_BLOCKS, NODE_SPARSE) = range(1, 17)
 
 FORWARD = 0
 BACKWARD = 1

@@ -39,6 +39,20 @@ struct BatchLaunch {
 };
 cudaError_t launch_batch(const BatchLaunch &b, cudaStream_t s);
 
+// one CSR sparse-times-columns launch (fm_sparse.cu): y[:, m] = S x[:, m]
+// for m < num_cols, S given by row pointers, column indices and values in
+// the compute element type; group = lanes per row (1, 2, ..., 32)
+struct SpStep {
+  const i64 *ptr = nullptr, *idx = nullptr;
+  const void *val = nullptr;
+  const void *src = nullptr;
+  void *dst = nullptr;
+  int src_type = 0, dst_type = 0;
+  i64 ld_src = 0, ld_dst = 0, rows = 0, num_cols = 0;
+};
+cudaError_t launch_spmv(int ctype, const SpStep &p, int group,
+                        cudaStream_t s);
+
 // largest FFT radix the kernels of a compute type are built with (see
 // MinBlocks / Radix16 in fm_vprog.cuh): 8 for single precision and
 // double-float, 16 otherwise

@@ -201,8 +201,14 @@ struct LStep {
   int src, dst;  // 0 = x, 1 = y, >= 2 scratch
   // first row of the launch's operand inside its buffer (Blocks segments)
   i64 src_off = 0, dst_off = 0;
-  int cls, threads;
-  size_t smem;
+  // 0: vector program (vprog_kernel); 1: CSR sparse product (spmv_kernel)
+  int kind = 0;
+  const i64 *sp_ptr = nullptr, *sp_idx = nullptr;
+  const void *sp_val = nullptr;
+  i64 sp_rows = 0;
+  int sp_group = 32;
+  int cls = 0, threads = 0;
+  size_t smem = 0;
   int lay = 0;                     // tile layout (1: element-major)
   int ept = 8;                     // elements per thread of its class
   int tma_in_ok = 0, tma_out_ok = 0;  // views allow TMA boxes
@@ -284,7 +290,7 @@ struct Unit;
 typedef std::vector<Unit> Chain;
 
 struct Unit {
-  enum Kind { PROG, STEPS, SUM, BLOCKS } kind = PROG;
+  enum Kind { PROG, STEPS, SUM, BLOCKS, SPARSE } kind = PROG;
   i64 n_in = 0, n_out = 0;
   // PROG
   std::vector<fmk::Op> ops;
@@ -299,6 +305,10 @@ struct Unit {
   std::vector<std::vector<Chain>> grid;
   std::vector<std::vector<int>> has;
   std::vector<i64> seg_in, seg_out;
+  // SPARSE: CSR of the operator (or of its adjoint) on the device
+  const i64 *sp_ptr = nullptr, *sp_idx = nullptr;
+  const void *sp_val = nullptr;
+  int sp_group = 32;
 };
 
 struct NodeRec {
@@ -1213,6 +1223,7 @@ class Planner {
         c.push_back(u);
         return c;
       }
+      case FM_NODE_SPARSE: return sparse(d, fwd);
       case FM_NODE_HERMITIAN: return compile(r.ch.at(0), !fwd);
       case FM_NODE_CONJUGATE: {
         c.push_back(prog({mkop(fmk::OP_CONJ, (int)n_in)}, n_in, n_in, n_in));
@@ -1281,6 +1292,65 @@ class Planner {
       fused.push_back(out[i]);
     }
     return fused;
+  }
+
+  // CSR product (fastmat/Sparse.pyx): forward uses the node's CSR, the
+  // adjoint its conjugate transpose, built here as a second CSR (entries of
+  // a row in ascending source-row order)
+  Chain sparse(const fm_node &d, bool fwd) {
+    const i64 R = d.rows, C = d.cols, nnz = d.n;
+    if (nnz < 0 || d.len0 != nnz || d.len1 != R + 1 + nnz)
+      fail(FM_ERR_VALUE, "Sparse: inconsistent CSR arrays");
+    const std::vector<cd> val = nnz ? node_vec(d, 0) : std::vector<cd>();
+    const std::vector<i64> iv = node_idx(d, 1);
+    if (iv[0] != 0 || iv[(size_t)R] != nnz)
+      fail(FM_ERR_VALUE, "Sparse: row pointers must run from 0 to nnz");
+    for (i64 r = 0; r < R; ++r)
+      if (iv[(size_t)r + 1] < iv[(size_t)r])
+        fail(FM_ERR_VALUE, "Sparse: row pointers must not decrease");
+    for (i64 k = 0; k < nnz; ++k) {
+      const i64 c = iv[(size_t)(R + 1 + k)];
+      if (c < 0 || c >= C) fail(FM_ERR_VALUE, "Sparse: column index out of range");
+    }
+    std::vector<i64> ptr, idx;
+    std::vector<cd> v;
+    if (fwd) {
+      ptr.assign(iv.begin(), iv.begin() + (R + 1));
+      idx.assign(iv.begin() + (R + 1), iv.end());
+      v = val;
+    } else {
+      ptr.assign((size_t)C + 1, 0);
+      for (i64 k = 0; k < nnz; ++k) ++ptr[(size_t)iv[(size_t)(R + 1 + k)] + 1];
+      for (i64 c = 0; c < C; ++c) ptr[(size_t)c + 1] += ptr[(size_t)c];
+      std::vector<i64> fill(ptr.begin(), ptr.end() - 1);
+      idx.assign((size_t)nnz, 0);
+      v.assign((size_t)nnz, cd(0.0, 0.0));
+      for (i64 r = 0; r < R; ++r)
+        for (i64 k = iv[(size_t)r]; k < iv[(size_t)r + 1]; ++k) {
+          const i64 c = iv[(size_t)(R + 1 + k)];
+          const i64 at = fill[(size_t)c]++;
+          idx[(size_t)at] = r;
+          v[(size_t)at] = std::conj(val[(size_t)k]);
+        }
+    }
+    const i64 rows = fwd ? R : C;
+    if (idx.empty()) {  // keep the device arrays non-empty
+      idx.push_back(0);
+      v.push_back(cd(0.0, 0.0));
+    }
+    Unit u;
+    u.kind = Unit::SPARSE;
+    u.n_in = fwd ? C : R;
+    u.n_out = rows;
+    u.sp_ptr = upload_map(ptr);
+    u.sp_idx = upload_map(idx);
+    u.sp_val = upload(v);
+    // lanes per row: the mean row length rounded up to a power of two
+    const i64 mean = rows > 0 ? (nnz + rows - 1) / rows : 1;
+    int g = 1;
+    while (g < 32 && g < mean) g *= 2;
+    u.sp_group = g;
+    return Chain{u};
   }
 
   Chain kron(const NodeRec &r, bool fwd) {
@@ -1662,6 +1732,20 @@ class Planner {
           }
           break;
         }
+        case Unit::SPARSE: {
+          LStep ls;
+          ls.kind = 1;
+          ls.src = cur;
+          ls.dst = dst;
+          ls.st = base_step();
+          ls.sp_ptr = u.sp_ptr;
+          ls.sp_idx = u.sp_idx;
+          ls.sp_val = u.sp_val;
+          ls.sp_rows = u.n_out;
+          ls.sp_group = u.sp_group;
+          out.push_back(ls);
+          break;
+        }
         case Unit::BLOCKS: {
           // output segment o = sum over q of block (o, q) applied to input
           // segment q: the first block writes, later ones go through
@@ -1779,6 +1863,22 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 
 // Finish a bound launch (TMA descriptors, status word) and issue it.
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
+  if (ls.kind == 1) {
+    fmk::SpStep sp;
+    sp.ptr = ls.sp_ptr;
+    sp.idx = ls.sp_idx;
+    sp.val = ls.sp_val;
+    sp.src = st.src;
+    sp.dst = st.dst;
+    sp.src_type = st.src_type;
+    sp.dst_type = st.dst_type;
+    sp.ld_src = st.ld_src;
+    sp.ld_dst = st.ld_dst;
+    sp.rows = ls.sp_rows;
+    sp.num_cols = st.num_cols;
+    CUDA_TRY(fmk::launch_spmv(P->ctype, sp, ls.sp_group, s));
+    return;
+  }
   st.err = P->err;
   st.tma_in = st.tma_out = 0;
   if (ls.lay == 0 || ls.lay == 2) {
@@ -2189,6 +2289,7 @@ int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,
     if (launch < 0 || launch >= (int)steps.size())
       fail(FM_ERR_VALUE, "launch index out of range");
     LStep &ls = steps[launch];
+    if (ls.kind != 0) return FM_OK;  // no tile shape to set
     const LStep keep = ls;
     if (!configure(plan->esz, ls, vectors_per_tile, nbuf, true, ls.lay)) {
       ls = keep;
@@ -2211,6 +2312,7 @@ int fm_plan_set_tile_layout(fm_plan *plan, int32_t direction, int32_t launch,
       fail(FM_ERR_VALUE, "launch index out of range");
     if (layout < 0 || layout > 2) fail(FM_ERR_VALUE, "invalid layout");
     LStep &ls = steps[launch];
+    if (ls.kind != 0) return FM_OK;  // no tile shape to set
     const LStep keep = ls;
     if (!configure(plan->esz, ls, vectors_per_tile, nbuf, true, layout)) {
       ls = keep;
@@ -2258,6 +2360,7 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
     void *tsrc = nullptr, *tdst = nullptr;
     try {
       for (LStep &ls : plan->steps[direction]) {
+        if (ls.kind != 0) continue;  // sparse products have no tile shape
         const i64 rs = rows_of(ls.src), rd = rows_of(ls.dst);
         // a sample of the columns, at most ~512 MiB per operand
         const i64 cap = std::max<i64>(
@@ -2372,6 +2475,13 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
     char line[512];
     for (const LStep &ls : plan->steps[direction]) {
       const fmk::Step &st = ls.st;
+      if (ls.kind == 1) {
+        snprintf(line, sizeof(line),
+                 "launch src=%d dst=%d sparse rows=%lld lanes_per_row=%d\n",
+                 ls.src, ls.dst, ls.sp_rows, ls.sp_group);
+        s += line;
+        continue;
+      }
       snprintf(line, sizeof(line),
                "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,%lld) "
                "L=%d B=%d threads=%d smem=%zu cls=%d acc=%d:",
@@ -2470,6 +2580,9 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
       }
       int level = 0;
       for (const LStep &ls0 : P->steps[dir]) {
+        if (ls0.kind != 0)
+          fail(FM_ERR_UNSUPPORTED, "fm_batch_create: sparse operators run "
+                                   "outside batches");
         LStep ls = ls0;
         if (!configure(esz, ls, 0, 0, false, 0, false))
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "

@@ -714,3 +714,42 @@ class BlockDiag(Matrix):
             r += t.numRows
             c += t.numCols
         return out
+
+
+class Sparse(Matrix):
+    """A scipy.sparse matrix as an operator (fastmat/Sparse.pyx:25-185),
+    applied on the GPU as a CSR product; the adjoint is the conjugate
+    transpose, stored as a second CSR when the plan is built."""
+
+    def __init__(self, matSparse, **options):
+        import scipy.sparse as sps
+        if not sps.issparse(matSparse):
+            raise TypeError("Sparse: Use Matrix() for numpy ndarrays."
+                            if isinstance(matSparse, np.ndarray)
+                            else "Sparse: Matrix is not a scipy spmatrix")
+        self._spArray = matSparse.tocsr()
+        self._spArrayH = None
+        self._init_properties(self._spArray.shape[0],
+                              self._spArray.shape[1],
+                              T.supported(self._spArray.dtype), **options)
+
+    @property
+    def spArray(self):
+        return self._spArray
+
+    @property
+    def spArrayH(self):
+        if self._spArrayH is None:
+            self._spArrayH = self._spArray.T.conj().tocsr()
+        return self._spArrayH
+
+    def _emit(self, b):
+        a = self._spArray
+        data = np.asarray(a.data).astype(self.dtype, copy=False)
+        idx = np.concatenate([np.asarray(a.indptr, dtype=np.int64),
+                              np.asarray(a.indices, dtype=np.int64)])
+        return b.add(_native.NODE_SPARSE, self, n=int(a.nnz),
+                     vec0=data if data.size else None, vec1=idx, int1=True)
+
+    def _reference(self):
+        return self._spArray.toarray().astype(self.dtype, copy=False)

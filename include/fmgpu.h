@@ -87,6 +87,10 @@ extern "C" {
                                   holds at least one block); blocks of a row
                                   share their height, of a column their
                                   width (fastmat's Blocks and BlockDiag)     */
+#define FM_NODE_SPARSE 16      /* CSR matrix: n = number of nonzeros, vec0 =
+                                  the n values, vec1 = int64 row pointers
+                                  (rows + 1) followed by the n column
+                                  indices (len1 = rows + 1 + n)             */
 
 typedef struct fm_node {
     int32_t kind;

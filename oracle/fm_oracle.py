@@ -492,6 +492,41 @@ class Blocks(Op):
                          for r in self.rows])
 
 
+class Sparse(Op):
+    """fastmat/Sparse.pyx:25-185: a CSR matrix; forward S x, backward
+    S^H x.  Restated with the CSR arrays (row of every nonzero from the row
+    pointers, products scattered into the rows with np.add.at) rather than
+    scipy's product."""
+
+    def __init__(self, mat):
+        a = mat.tocsr()
+        self.shape = a.shape
+        self.dtype = np.dtype(a.dtype).type
+        self.val = np.asarray(a.data)
+        self.col = np.asarray(a.indices, dtype=np.int64)
+        self.row = np.repeat(np.arange(a.shape[0], dtype=np.int64),
+                             np.diff(np.asarray(a.indptr, dtype=np.int64)))
+
+    def _fwd(self, x):
+        dt = self.out_dtype(x.dtype)
+        y = np.zeros((self.shape[0], x.shape[1]), dt)
+        np.add.at(y, self.row, self.val[:, None].astype(dt) *
+                  x[self.col].astype(dt))
+        return y
+
+    def _bwd(self, x):
+        dt = self.out_dtype(x.dtype)
+        y = np.zeros((self.shape[1], x.shape[1]), dt)
+        np.add.at(y, self.col, np.conj(self.val)[:, None].astype(dt) *
+                  x[self.row].astype(dt))
+        return y
+
+    def dense(self):
+        a = np.zeros(self.shape, np.complex128)
+        np.add.at(a, (self.row, self.col), self.val)
+        return a
+
+
 class BlockDiag(Op):
     """fastmat/BlockDiag.pyx:95-200: operators along the block diagonal."""
 

@@ -46,7 +46,7 @@ def load_accessors():
     data = np.load(os.path.join(HERE, 'accessors.npz'))
     out = {}
     for k in data.files:
-        name, key = k.split('__')
+        name, key = k.split('__', 1)
         out.setdefault(name, {})[key] = data[k]
     return out
 

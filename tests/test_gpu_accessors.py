@@ -6,6 +6,7 @@ the solver-backed ``Inverse`` / ``PseudoInverse``
 (fastmat/inspect/test.py:444-700 test the same accessors)."""
 
 import numpy as np
+from scipy.sparse import csr_matrix
 import pytest
 
 from oracle import fm_oracle as fo
@@ -25,7 +26,8 @@ def _ns():
                 Permutation=fg.Permutation, Product=fg.Product, Sum=fg.Sum,
                 Hermitian=fg.Hermitian, Conjugate=fg.Conjugate,
                 Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix,
-                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
+                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag,
+                Sparse=fg.Sparse, csr=csr_matrix, np=np)
 
 
 def _tol(ref):
@@ -80,8 +82,16 @@ def test_norms_and_normalized(case):
     if 'colnormalized' in acc:
         assert fo.rel_err(op.colNormalized.array,
                           acc['colnormalized']) <= 1e-12
+    if 'rownormalized' in acc:
         assert fo.rel_err(op.rowNormalized.array,
                           acc['rownormalized']) <= 1e-12
+    # zero-norm columns / rows: the reference raises, so must we
+    if 'colnormalized_raises' in acc:
+        with pytest.raises(ValueError):
+            op.colNormalized
+    if 'rownormalized_raises' in acc:
+        with pytest.raises(ValueError):
+            op.rowNormalized
 
 
 def test_getitem_forms():

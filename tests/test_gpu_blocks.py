@@ -110,3 +110,51 @@ def test_blockdiag_in_a_batch():
     outs = fg.Batch(items).run()
     for y, ref in zip(outs, refs):
         assert fo.rel_err(y.cpu().numpy(), ref) <= 1e-11
+
+
+def test_sparse_shapes_types_and_composites():
+    """fastmat/Sparse.pyx: CSR products in both directions, every lane
+    group width, empty rows and columns, integer wrap-around, and sparse
+    factors inside Blocks / Product / Sum."""
+    import scipy.sparse as sps
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(25)
+    for rows, cols, dens in [(1, 1, 1.0), (300, 7, 0.3), (7, 3000, 0.4),
+                             (500, 400, 0.01), (64, 64, 0.0),
+                             (1000, 1000, 0.03)]:
+        a = (sps.random(rows, cols, density=dens, random_state=rng) +
+             1j * sps.random(rows, cols, density=dens, random_state=rng))
+        S, O = fg.Sparse(a), fo.Sparse(a)
+        x = _c(rng, cols, 3)
+        g = _c(rng, rows, 2)
+        ref = O.forward(x)
+        y = S.forward(x)
+        assert y.dtype == np.complex128
+        assert fo.rel_err(y, ref) <= 1e-12 or np.abs(ref).max() == 0
+        assert fo.rel_err(S.backward(g), O.backward(g)) <= 1e-12 or (
+            np.abs(O.backward(g)).max() == 0)
+    # integers wrap like fastmat's typed loops
+    ai = sps.random(40, 30, density=0.5, random_state=rng,
+                    data_rvs=lambda k: rng.integers(-100, 100, k)).astype(
+                        np.int8)
+    xi = rng.integers(-100, 100, (30, 4)).astype(np.int8)
+    yi = fg.Sparse(ai).forward(xi)
+    assert yi.dtype == np.int8
+    assert np.array_equal(yi, fo.Sparse(ai).forward(xi))
+    # in composites
+    a = sps.random(50, 50, density=0.1, random_state=rng).astype(np.complex128)
+    c = _c(rng, 50)
+    S, O = fg.Sparse(a), fo.Sparse(a)
+    B = fg.Blocks([[S, fg.Circulant(c)], [fg.Eye(50), S.H]])
+    OB = fo.Blocks([[O, fo.Circulant(c)], [fo.Eye(50), fo.Hermitian(O)]])
+    x = _c(rng, 100, 5)
+    assert fo.rel_err(B.forward(x), OB.forward(x)) <= 1e-12
+    assert fo.rel_err(B.backward(x), OB.backward(x)) <= 1e-12
+    P = fg.Sum(fg.Product(S, fg.Fourier(50)), fg.Diag(c))
+    OP = fo.Sum(fo.Product(O, fo.Fourier(50)), fo.Diag(c))
+    assert fo.rel_err(P.forward(x[:50]), OP.forward(x[:50])) <= 1e-12
+    # single precision
+    S32 = fg.Sparse(a, precision='fp32')
+    y32 = S32.forward(x[:50].astype(np.complex64))
+    assert y32.dtype == np.complex64
+    assert fo.rel_err(y32, O.forward(x[:50])) <= tolerance(y32, x[:50])

@@ -2,6 +2,7 @@
 CPU oracle, for every operator case in tests/golden/operators.npz."""
 
 import numpy as np
+from scipy.sparse import csr_matrix
 import pytest
 
 from oracle import fm_oracle as fo
@@ -21,7 +22,8 @@ def _ns():
                 Permutation=fg.Permutation, Product=fg.Product, Sum=fg.Sum,
                 Hermitian=fg.Hermitian, Conjugate=fg.Conjugate,
                 Transpose=fg.Transpose, Eye=fg.Eye, Matrix=fg.Matrix,
-                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
+                Blocks=fg.Blocks, BlockDiag=fg.BlockDiag,
+                Sparse=fg.Sparse, csr=csr_matrix, np=np)
 
 
 ONS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
@@ -29,7 +31,8 @@ ONS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
            Partial=fo.Partial, Permutation=fo.Permutation,
            Product=fo.Product, Sum=fo.Sum, Hermitian=fo.Hermitian,
            Conjugate=fo.Conjugate, Transpose=fo.Transpose, Eye=fo.Eye,
-           Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag, np=np)
+           Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag,
+           Sparse=fo.Sparse, csr=csr_matrix, np=np)
 
 
 def _close(out, ref, x, name=None):

@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+from scipy.sparse import csr_matrix
 import pytest
 
 import fastmat_gb300 as fg
@@ -21,7 +22,8 @@ NS = dict(Fourier=fg.Fourier, Circulant=fg.Circulant, Toeplitz=fg.Toeplitz,
           Partial=fg.Partial, Permutation=fg.Permutation,
           Product=fg.Product, Sum=fg.Sum, Hermitian=fg.Hermitian,
           Conjugate=fg.Conjugate, Transpose=fg.Transpose, Eye=fg.Eye,
-          Matrix=fg.Matrix, Blocks=fg.Blocks, BlockDiag=fg.BlockDiag, np=np)
+          Matrix=fg.Matrix, Blocks=fg.Blocks, BlockDiag=fg.BlockDiag,
+          Sparse=fg.Sparse, csr=csr_matrix, np=np)
 
 
 @pytest.mark.parametrize('case', CASES, ids=lambda c: c.name)

@@ -2,6 +2,7 @@
 """
 
 import numpy as np
+from scipy.sparse import csr_matrix
 import pytest
 
 from oracle import fm_oracle as fo
@@ -15,7 +16,8 @@ NS = dict(Fourier=fo.Fourier, Circulant=fo.Circulant, Toeplitz=fo.Toeplitz,
           Partial=fo.Partial, Permutation=fo.Permutation,
           Product=fo.Product, Sum=fo.Sum, Hermitian=fo.Hermitian,
           Conjugate=fo.Conjugate, Transpose=fo.Transpose, Eye=fo.Eye,
-          Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag, np=np)
+          Matrix=fo.Dense, Blocks=fo.Blocks, BlockDiag=fo.BlockDiag,
+           Sparse=fo.Sparse, csr=csr_matrix, np=np)
 
 
 def expected_dtype(op_dtype, x_dtype):
@@ -69,8 +71,13 @@ def test_oracle_pins_accessor_fixtures(case):
                        rtol=1e-12, atol=1e-12 * scale)
     if 'colnormalized' in acc:
         assert close(acc['colnormalized'] * np.linalg.norm(d, axis=0), d)
+    if 'rownormalized' in acc:
         assert close(acc['rownormalized'] *
                      np.linalg.norm(d, axis=1)[:, None], d)
+    if 'colnormalized_raises' in acc:
+        assert np.any(np.linalg.norm(d, axis=0) == 0)
+    if 'rownormalized_raises' in acc:
+        assert np.any(np.linalg.norm(d, axis=1) == 0)
 
 
 def test_fft_size_heuristics_match_reference():
