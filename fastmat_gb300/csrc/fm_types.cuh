@@ -78,6 +78,48 @@ __device__ __forceinline__ dfc cmulc(dfc a, dfc b) {
   return dfc{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
 }
 
+// Unnormalised double-float, for the additions inside one butterfly: the
+// head is the rounded sum of the heads (TwoSum keeps its rounding error
+// exactly) and the tail collects tails and errors without renormalising,
+// 8 FP32 operations per addition instead of 11; a product skips the final
+// renormalisation too (4 instead of 7).  Tails stay a few units of 2^-24
+// of the magnitudes that entered the chain, so a chain of k operations
+// keeps the norm-wise error bound of about k 2^-48 times the sum of those
+// magnitudes (the bound an FFT error analysis uses).  Values are
+// renormalised (Fast2Sum) when they leave the butterfly.
+struct dfu {
+  float h, l;
+  dfu() = default;
+  __host__ __device__ constexpr dfu(float h_, float l_) : h(h_), l(l_) {}
+  __host__ __device__ constexpr dfu(double d)
+      : h((float)d), l((float)(d - (double)(float)d)) {}
+};
+struct dfcu {
+  dfu x, y;
+};
+__device__ __forceinline__ dfu operator+(dfu a, dfu b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float e = (a.h - (s - bb)) + (b.h - bb);
+  return dfu(s, (a.l + b.l) + e);
+}
+__device__ __forceinline__ dfu operator-(dfu a) { return dfu(-a.h, -a.l); }
+__device__ __forceinline__ dfu operator-(dfu a, dfu b) { return a + (-b); }
+__device__ __forceinline__ dfu operator*(dfu a, dfu b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return dfu(p, e);
+}
+__device__ __forceinline__ dfu smul(int s, dfu a) { return s < 0 ? -a : a; }
+__device__ __forceinline__ dfcu operator+(dfcu a, dfcu b) {
+  return dfcu{a.x + b.x, a.y + b.y};
+}
+__device__ __forceinline__ dfcu operator-(dfcu a, dfcu b) {
+  return dfcu{a.x - b.x, a.y - b.y};
+}
+
 // double -> double-float with integer operations only (the FP64 pipe of
 // this GPU is slow): h is d rounded to 24 bits, l the float nearest to the
 // exact remainder d - h.  Zeros, subnormals and values outside the float
@@ -159,6 +201,32 @@ template <> struct Tr<dfc> {
   static constexpr int code = FM_C128;
   typedef df R;
 };
+template <> struct Tr<dfu> {
+  static constexpr bool cplx = false;
+  static constexpr int code = FM_F64;
+  typedef dfu R;
+};
+template <> struct Tr<dfcu> {
+  static constexpr bool cplx = true;
+  static constexpr int code = FM_C128;
+  typedef dfu R;
+};
+// the type a butterfly computes in: unnormalised for double-float
+template <class C> struct Lazy { typedef C type; };
+template <> struct Lazy<df> { typedef dfu type; };
+template <> struct Lazy<dfc> { typedef dfcu type; };
+template <class C> __device__ __forceinline__ C to_lazy(C a) { return a; }
+template <class C> __device__ __forceinline__ C from_lazy(C a) { return a; }
+__device__ __forceinline__ dfu to_lazy(df a) { return dfu(a.h, a.l); }
+__device__ __forceinline__ dfcu to_lazy(dfc a) {
+  return dfcu{dfu(a.x.h, a.x.l), dfu(a.y.h, a.y.l)};
+}
+__device__ __forceinline__ df from_lazy(dfu a) {
+  return fast_two_sum(a.h, a.l);
+}
+__device__ __forceinline__ dfc from_lazy(dfcu a) {
+  return dfc{fast_two_sum(a.x.h, a.x.l), fast_two_sum(a.y.h, a.y.l)};
+}
 template <class E> struct Emu { static constexpr bool v = false; };
 template <> struct Emu<df> { static constexpr bool v = true; };
 template <> struct Emu<dfc> { static constexpr bool v = true; };
@@ -226,6 +294,10 @@ __device__ __forceinline__ df addv(df a, df b) { return a + b; }
 __device__ __forceinline__ dfc addv(dfc a, dfc b) { return a + b; }
 __device__ __forceinline__ df subv(df a, df b) { return a - b; }
 __device__ __forceinline__ dfc subv(dfc a, dfc b) { return a - b; }
+__device__ __forceinline__ dfu addv(dfu a, dfu b) { return a + b; }
+__device__ __forceinline__ dfcu addv(dfcu a, dfcu b) { return a + b; }
+__device__ __forceinline__ dfu subv(dfu a, dfu b) { return a - b; }
+__device__ __forceinline__ dfcu subv(dfcu a, dfcu b) { return a - b; }
 
 __device__ __forceinline__ float conjv(float a) { return a; }
 __device__ __forceinline__ double conjv(double a) { return a; }

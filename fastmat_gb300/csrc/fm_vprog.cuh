@@ -467,10 +467,15 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
       }
     }
     if constexpr ((R & (R - 1)) == 0) {
-      dif_stages<R, R / 2>(v, sign);  // v[i] = output brev(i)
+      // the butterflies run in the unnormalised form of double-float
+      typedef typename Lazy<C>::type LC;
+      LC u[R];
+#pragma unroll
+      for (int n = 0; n < R; ++n) u[n] = to_lazy(v[n]);
+      dif_stages<R, R / 2>(u, sign);  // u[i] = output brev(i)
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        C y = v[i];
+        C y = from_lazy(u[i]);
         if constexpr (!DIT) {
           if (brev<R>(i) != 0) {  // folded by the unrolled loop
             const C w = twt[brev<R>(i) * tstep];
@@ -603,22 +608,26 @@ __device__ __forceinline__ void fwht_pass(E *sm, int Lp, int B, int Lf, int s,
       }
       const int base = ((q >> s) << (s + K)) | (q & lomask);
       E *vec = vbase<E, LAY>(sm, b, Lp);
-      E v[R];
+      // unnormalised double-float inside the group (see dfu)
+      typedef typename Lazy<E>::type LE;
+      LE v[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = vec[jx<E, LAY>(base + (r << s), B)];
+      for (int r = 0; r < R; ++r)
+        v[r] = to_lazy(vec[jx<E, LAY>(base + (r << s), B)]);
 #pragma unroll
       for (int h = 1; h < R; h <<= 1) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if ((r & h) == 0) {
-            const E a = v[r], c = v[r + h];
+            const LE a = v[r], c = v[r + h];
             v[r] = addv(a, c);
             v[r + h] = subv(a, c);
           }
         }
       }
 #pragma unroll
-      for (int r = 0; r < R; ++r) vec[jx<E, LAY>(base + (r << s), B)] = v[r];
+      for (int r = 0; r < R; ++r)
+        vec[jx<E, LAY>(base + (r << s), B)] = from_lazy(v[r]);
     }
   }
   group_sync(T);
