@@ -428,6 +428,27 @@ __device__ __forceinline__ void group_sync(int T) {
     __syncthreads();
 }
 
+// a * w (SG < 0) or a * conj(w) (SG > 0) for a butterfly value a in the
+// butterfly's computing type and a twiddle w (unnormalised products and
+// sums for double-float; the plain complex product otherwise)
+template <int SG, class LC, class C>
+__device__ __forceinline__ LC cmul_lazy(LC a, C w) {
+  if constexpr (std::is_same<LC, C>::value) {
+    return SG < 0 ? cmul(a, w) : cmulc(a, w);
+  } else {
+    const LC b = to_lazy(w);
+    LC r;
+    if constexpr (SG < 0) {
+      r.x = a.x * b.x - a.y * b.y;
+      r.y = a.x * b.y + a.y * b.x;
+    } else {
+      r.x = a.x * b.x + a.y * b.y;
+      r.y = a.y * b.x - a.x * b.y;
+    }
+    return r;
+  }
+}
+
 template <int R, bool DIT, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
                                           int Mprev,
@@ -459,32 +480,36 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
     C v[R];
 #pragma unroll
     for (int n = 0; n < R; ++n) v[n] = vec[jx<C, LAY>(base + M * n, B)];
-    if constexpr (DIT) {
-#pragma unroll
-      for (int k = 1; k < R; ++k) {
-        const C w = twt[k * tstep];
-        v[k] = sign < 0 ? cmul(v[k], w) : cmulc(v[k], w);
-      }
-    }
     if constexpr ((R & (R - 1)) == 0) {
-      // the butterflies run in the unnormalised form of double-float
+      // twiddles and butterflies run in the unnormalised form of
+      // double-float (one renormalisation per output element)
       typedef typename Lazy<C>::type LC;
       LC u[R];
 #pragma unroll
       for (int n = 0; n < R; ++n) u[n] = to_lazy(v[n]);
+      if constexpr (DIT) {
+#pragma unroll
+        for (int k = 1; k < R; ++k)
+          u[k] = cmul_lazy<sign>(u[k], twt[k * tstep]);
+      }
       dif_stages<R, R / 2>(u, sign);  // u[i] = output brev(i)
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        C y = from_lazy(u[i]);
+        LC y = u[i];
         if constexpr (!DIT) {
-          if (brev<R>(i) != 0) {  // folded by the unrolled loop
-            const C w = twt[brev<R>(i) * tstep];
-            y = sign < 0 ? cmul(y, w) : cmulc(y, w);
-          }
+          if (brev<R>(i) != 0)  // folded by the unrolled loop
+            y = cmul_lazy<sign>(y, twt[brev<R>(i) * tstep]);
         }
-        vec[jx<C, LAY>(base + M * brev<R>(i), B)] = y;
+        vec[jx<C, LAY>(base + M * brev<R>(i), B)] = from_lazy(y);
       }
     } else {
+      if constexpr (DIT) {
+#pragma unroll
+        for (int k = 1; k < R; ++k) {
+          const C w = twt[k * tstep];
+          v[k] = sign < 0 ? cmul(v[k], w) : cmulc(v[k], w);
+        }
+      }
       dft<R>(v, sign);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
