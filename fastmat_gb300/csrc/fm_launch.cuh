@@ -34,6 +34,7 @@ struct BatchLaunch {
   unsigned *bar = nullptr;      // grid-barrier counter, zero at launch
   int *err = nullptr;
   int max_B = 1;
+  size_t max_tile = 0;  // bytes of the largest tile (one of two slots)
   size_t smem = 0;
   long long max_level_tiles = 1;
 };

@@ -2653,9 +2653,8 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
     }
     max_level_tiles = std::max(max_level_tiles, level_tiles);
     level.push_back((int)items.size());
-    const size_t head =
-        ((sizeof(fmk::VInfo) + 12) * (size_t)max_B + 127) / 128 * 128;
-    const size_t smem = head + max_tile;
+    // two slots: the next tile loads while the current one is transformed
+    const size_t smem = fmk::batch_smem(max_B, max_tile);
     if (smem > (size_t)fmk::kMaxSmem)
       fail(FM_ERR_UNSUPPORTED, "fm_batch_create: tile too large");
     fmk::Step *dsteps = nullptr;
@@ -2684,6 +2683,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
     L.bar = reinterpret_cast<unsigned *>(B->status);
     L.err = B->status + 1;
     L.max_B = max_B;
+    L.max_tile = max_tile;
     L.smem = smem;
     L.max_level_tiles = max_level_tiles;
     B->num_steps = (i64)steps.size();

@@ -1726,35 +1726,117 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target,
   return ok != 0;
 }
 
+// shared memory of the batch kernel: two slots of launch records, the
+// per-vector scalars, two slots of (per-vector records, per-vector
+// exponents) and two tile buffers
+__host__ __device__ __forceinline__ size_t batch_steps_bytes() {
+  return (2 * sizeof(Step) + 127) / 128 * 128;
+}
+__host__ __device__ __forceinline__ size_t batch_head_bytes(int max_B) {
+  return batch_steps_bytes() +
+         ((size_t)max_B * (8 + 2 * (sizeof(VInfo) + 4)) + 127) / 128 * 128;
+}
+__host__ __device__ __forceinline__ size_t batch_smem(int max_B,
+                                                      size_t max_tile) {
+  return batch_head_bytes(max_B) + 2 * max_tile;
+}
+
+// Loads of one batch tile into a slot: cp.async when the source already
+// has the compute type and needs no gather (completion is awaited later,
+// so the copy overlaps the previous tile's program), synchronous loads with
+// conversion and gather otherwise.
+// The launch record is first copied into shared memory (read there by
+// every op of the tile program instead of from global memory).
+template <class E>
+__device__ __forceinline__ void batch_issue_load(const Step *gp, Step *slot,
+                                                 E *sm, VInfo *vi, i64 tile,
+                                                 int tid, int T) {
+  {
+    static_assert(sizeof(Step) % 16 == 0, "launch record size");
+    const int4 *src = reinterpret_cast<const int4 *>(gp);
+    int4 *dst = reinterpret_cast<int4 *>(slot);
+    for (int i = tid; i < (int)(sizeof(Step) / 16); i += T) dst[i] = src[i];
+  }
+  __syncthreads();
+  const Step &p = *slot;
+  const i64 nvec = p.V * p.num_cols;
+  const FDiv dV((unsigned)p.V), dci((unsigned)p.vin.Cc),
+      dco((unsigned)p.vout.Cc);
+  setup_tile(p, vi, tile, dV, dci, dco, nvec, tid, T);
+  __syncthreads();
+  if (p.src_type == Tr<E>::code && !p.map_in)
+    load_async<E, 0>(p, sm, vi, tid, T);
+  else
+    load_general<E, 0>(p, sm, vi, tid, T);
+  cp_async_commit();
+}
+
 template <class E, int CLS>
 __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
     batch_kernel(const Step *__restrict__ steps, const i64 *__restrict__ start,
                  const int *__restrict__ level, int nlev, unsigned *bar,
-                 int *err, int max_B) {
+                 int *err, int max_B, size_t max_tile) {
   extern __shared__ __align__(128) unsigned char fm_smem[];
   const int tid = threadIdx.x, T = blockDim.x;
-  VInfo *const vi = reinterpret_cast<VInfo *>(fm_smem);
-  i64 *sq = reinterpret_cast<i64 *>(vi + max_B);
-  int *sexp = reinterpret_cast<int *>(sq + max_B);
-  E *sm = reinterpret_cast<E *>(
-      fm_smem + ((sizeof(VInfo) * max_B + 8 * max_B + 4 * max_B + 127) &
-                 ~(size_t)127));
+  Step *const sst = reinterpret_cast<Step *>(fm_smem);
+  unsigned char *const h = fm_smem + batch_steps_bytes();
+  i64 *sq = reinterpret_cast<i64 *>(h);
+  // slot k: launch record, per-vector records, exponents and tile buffer
+  // (addresses recomputed on use to keep registers free)
+  const unsigned rec = (unsigned)((sizeof(VInfo) + 4) * max_B);
+  auto vis = [&](int k) {
+    return reinterpret_cast<VInfo *>(h + 8 * max_B + k * rec);
+  };
+  auto sexps = [&](int k) {
+    return reinterpret_cast<int *>(h + 8 * max_B + k * rec +
+                                   sizeof(VInfo) * max_B);
+  };
+  auto bufs = [&](int k) {
+    return reinterpret_cast<E *>(fm_smem + batch_head_bytes(max_B) +
+                                 k * max_tile);
+  };
+  const i64 G = gridDim.x;
   for (int l = 0; l < nlev; ++l) {
     const int s0 = level[l], s1 = level[l + 1];
     const i64 t1 = start[s1];
-    int k = s0;
-    for (i64 g = start[s0] + blockIdx.x; g < t1; g += gridDim.x) {
-      while (start[k + 1] <= g) ++k;
-      const Step &p = steps[k];
-      const i64 nvec = p.V * p.num_cols;
-      const FDiv dV((unsigned)p.V), dci((unsigned)p.vin.Cc),
-          dco((unsigned)p.vout.Cc);
-      setup_tile(p, vi, g - start[k], dV, dci, dco, nvec, tid, T);
-      if constexpr (Emu<E>::v)
-        for (int b = tid; b < p.B; b += T) sexp[b] = 0;
+    // two-slot pipeline: the loads of tile g + G are issued before tile g
+    // is transformed and stored
+    i64 g = start[s0] + blockIdx.x;
+    int kc = s0, cur = 0;
+    if (g < t1) {
+      while (start[kc + 1] <= g) ++kc;
+      batch_issue_load<E>(steps + kc, sst, bufs(0), vis(0), g - start[kc],
+                          tid, T);
+    }
+    for (; g < t1; g += G) {
+      const i64 gn = g + G;
+      int kn = kc;
+      if (gn < t1) {
+        while (start[kn + 1] <= gn) ++kn;
+        batch_issue_load<E>(steps + kn, sst + (cur ^ 1), bufs(cur ^ 1),
+                            vis(cur ^ 1), gn - start[kn], tid, T);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
       __syncthreads();
-      load_general<E, 0>(p, sm, vi, tid, T);
-      __syncthreads();
+      const Step &p = sst[cur];
+      E *sm = bufs(cur);
+      VInfo *vi = vis(cur);
+      int *sexp = sexps(cur);
+      const bool async = p.src_type == Tr<E>::code && !p.map_in;
+      if constexpr (Emu<E>::v) {
+        if (async) {
+          emu_in<E, 0>(p, sm, vi, sexp, tid, T);
+        } else {
+          for (int b = tid; b < p.B; b += T) sexp[b] = 0;
+        }
+        __syncthreads();
+      }
+      if (async && (p.conj_in || p.pre)) {
+        load_fixup<E, 0>(p, sm, vi, tid, T);
+        __syncthreads();
+      }
       const int nwarps = T >> 5;
       if (warp_mode<E, CLS, 0>(p.B, p.L, nwarps)) {
         const int w = tid >> 5, vw = p.B / nwarps;
@@ -1766,6 +1848,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       }
       store_tile<E, 0>(p, sm, vi, sexp, tid, T);
       __syncthreads();
+      cur ^= 1;
+      kc = kn;
     }
     if (l + 1 < nlev &&
         !grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err))
