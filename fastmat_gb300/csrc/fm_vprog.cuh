@@ -449,11 +449,14 @@ __device__ __forceinline__ LC cmul_lazy(LC a, C w) {
   }
 }
 
-template <int R, bool DIT, int LAY, int SG, class C>
-__device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
-                                          int Mprev,
-                                          const C *__restrict__ tw, int tid,
-                                          int T) {
+// UT: every twiddle of the stage is 1 (M = 1: the last DIF stage and the
+// first DIT stage, where t = 0 for every butterfly), so the products are
+// left out
+template <int R, bool DIT, int LAY, int SG, bool UT, class C>
+__device__ __forceinline__ void fft_stage_body(C *sm, int Lp, int B, int Lf,
+                                               int Mprev,
+                                               const C *__restrict__ tw,
+                                               int tid, int T) {
   constexpr int sign = SG;
   const int M = Mprev / R;
   const int nw = Lf / R;
@@ -487,7 +490,7 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
       LC u[R];
 #pragma unroll
       for (int n = 0; n < R; ++n) u[n] = to_lazy(v[n]);
-      if constexpr (DIT) {
+      if constexpr (DIT && !UT) {
 #pragma unroll
         for (int k = 1; k < R; ++k)
           u[k] = cmul_lazy<sign>(u[k], twt[k * tstep]);
@@ -496,7 +499,7 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         LC y = u[i];
-        if constexpr (!DIT) {
+        if constexpr (!DIT && !UT) {
           if (brev<R>(i) != 0)  // folded by the unrolled loop
             y = cmul_lazy<sign>(y, twt[brev<R>(i) * tstep]);
         }
@@ -523,6 +526,22 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
         vec[jx<C, LAY>(base + M * k, B)] = y;
       }
     }
+  }
+}
+
+template <int R, bool DIT, int LAY, int SG, class C>
+__device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
+                                          int Mprev,
+                                          const C *__restrict__ tw, int tid,
+                                          int T) {
+  if constexpr ((R & (R - 1)) == 0) {
+    if (Mprev == R)
+      fft_stage_body<R, DIT, LAY, SG, true>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+    else
+      fft_stage_body<R, DIT, LAY, SG, false>(sm, Lp, B, Lf, Mprev, tw, tid,
+                                             T);
+  } else {
+    fft_stage_body<R, DIT, LAY, SG, false>(sm, Lp, B, Lf, Mprev, tw, tid, T);
   }
   group_sync(T);
 }
