@@ -237,7 +237,9 @@ struct fm_plan {
   // host execution staging
   void *dx = nullptr, *dy = nullptr;
   size_t dx_cap = 0, dy_cap = 0;
-  cudaStream_t hstream = nullptr;
+  cudaStream_t hstream = nullptr;          // compute
+  cudaStream_t hin = nullptr, hout = nullptr;  // copies in / out
+  std::vector<cudaEvent_t> hev;          // chunk hand-over events
   int *err = nullptr;  // device status word written by bounded waits
   ~fm_plan();
 };
@@ -248,6 +250,9 @@ fm_plan::~fm_plan() {
   if (dx) cudaFree(dx);
   if (dy) cudaFree(dy);
   if (hstream) cudaStreamDestroy(hstream);
+  if (hin) cudaStreamDestroy(hin);
+  if (hout) cudaStreamDestroy(hout);
+  for (cudaEvent_t e : hev) cudaEventDestroy(e);
 }
 
 struct fm_batch {
@@ -2242,16 +2247,24 @@ int fm_execute_static(fm_plan *plan, int32_t direction, const void *x,
 int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
                     int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
                     int64_t ld_y, int64_t num_cols) {
-  return guarded([&]() {
+  // streams that may still hold copies into the caller's buffers are
+  // drained before any return
+  auto drain = [&]() {
+    if (!plan) return;
+    for (cudaStream_t st : {plan->hin, plan->hstream, plan->hout})
+      if (st) cudaStreamSynchronize(st);
+  };
+  const int st = guarded([&]() {
     if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
     if (!valid_type(x_type) || !valid_type(y_type))
       fail(FM_ERR_TYPE, "unsupported element type");
     if (num_cols <= 0) return FM_OK;
-    const size_t bx = (size_t)ld_x * num_cols * esize(x_type);
-    const size_t by = (size_t)ld_y * num_cols * esize(y_type);
-    if (!plan->hstream)
-      CUDA_TRY(cudaStreamCreateWithFlags(&plan->hstream,
-                                         cudaStreamNonBlocking));
+    if (!x || !y) fail(FM_ERR_VALUE, "x or y is NULL");
+    const size_t cx = (size_t)ld_x * esize(x_type);  // bytes per column
+    const size_t cy = (size_t)ld_y * esize(y_type);
+    const size_t bx = cx * (size_t)num_cols, by = cy * (size_t)num_cols;
+    for (cudaStream_t *st : {&plan->hstream, &plan->hin, &plan->hout})
+      if (!*st) CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
     if (bx > plan->dx_cap) {
       if (plan->dx) cudaFree(plan->dx);
       plan->dx = nullptr;
@@ -2266,17 +2279,42 @@ int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
       CUDA_TRY(cudaMalloc(&plan->dy, by));
       plan->dy_cap = by;
     }
-    CUDA_TRY(cudaMemcpyAsync(plan->dx, x, bx, cudaMemcpyHostToDevice,
-                             plan->hstream));
-    const int st = fm_execute(plan, direction, plan->dx, x_type, ld_x,
-                              plan->dy, y_type, ld_y, num_cols,
-                              plan->hstream);
-    if (st != FM_OK) return st;
-    CUDA_TRY(cudaMemcpyAsync(y, plan->dy, by, cudaMemcpyDeviceToHost,
-                             plan->hstream));
+    // column chunks of at least ~64 MiB of operands, at most 8
+    const i64 want = (i64)std::min<size_t>(
+        8, std::max<size_t>(1, (bx + by) / ((size_t)64 << 20)));
+    const i64 per = (num_cols + std::min<i64>(want, num_cols) - 1) /
+                    std::min<i64>(want, num_cols);
+    const i64 nch = (num_cols + per - 1) / per;
+    while ((i64)plan->hev.size() < 2 * nch) {
+      cudaEvent_t e;
+      CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      plan->hev.push_back(e);
+    }
+    for (i64 k = 0; k < nch; ++k) {
+      const i64 c0 = k * per, m = std::min(per, num_cols - c0);
+      cudaEvent_t ev_in = plan->hev[(size_t)(2 * k)];
+      cudaEvent_t ev_done = plan->hev[(size_t)(2 * k + 1)];
+      char *dxk = (char *)plan->dx + c0 * cx;
+      char *dyk = (char *)plan->dy + c0 * cy;
+      CUDA_TRY(cudaMemcpyAsync(dxk, (const char *)x + c0 * cx, m * cx,
+                               cudaMemcpyHostToDevice, plan->hin));
+      CUDA_TRY(cudaEventRecord(ev_in, plan->hin));
+      CUDA_TRY(cudaStreamWaitEvent(plan->hstream, ev_in, 0));
+      const int s2 = fm_execute(plan, direction, dxk, x_type, ld_x, dyk,
+                                y_type, ld_y, m, plan->hstream);
+      if (s2 != FM_OK) return s2;
+      CUDA_TRY(cudaEventRecord(ev_done, plan->hstream));
+      CUDA_TRY(cudaStreamWaitEvent(plan->hout, ev_done, 0));
+      CUDA_TRY(cudaMemcpyAsync((char *)y + c0 * cy, dyk, m * cy,
+                               cudaMemcpyDeviceToHost, plan->hout));
+    }
+    CUDA_TRY(cudaStreamSynchronize(plan->hout));
     CUDA_TRY(cudaStreamSynchronize(plan->hstream));
+    CUDA_TRY(cudaStreamSynchronize(plan->hin));
     return fm_plan_check(plan);
   });
+  if (st != FM_OK) drain();
+  return st;
 }
 
 int fm_plan_set_tile(fm_plan *plan, int32_t direction, int32_t launch,

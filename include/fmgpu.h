@@ -196,7 +196,10 @@ int fm_execute_static(fm_plan *plan, int32_t direction,
                       int64_t num_cols, void *stream);
 
 /* Same as fm_execute with HOST buffers: copies x to the device, runs the
- * plan and copies the result back into y before returning (synchronous). */
+ * plan and copies the result back into y before returning (synchronous).
+ * Large calls are split into column chunks pipelined over three streams
+ * (copy in, compute, copy out), so with page-locked host buffers the
+ * copies of one chunk overlap the transform of the next. */
 int fm_execute_host(fm_plan *plan, int32_t direction,
                     const void *x, int32_t x_type, int64_t ld_x,
                     void *y, int32_t y_type, int64_t ld_y,
