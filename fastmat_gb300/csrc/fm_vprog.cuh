@@ -336,11 +336,15 @@ template <int R> __host__ __device__ constexpr int brev(int i) {
 // Unsigned division by a runtime divisor 1 <= d < 2^31 for dividends below
 // 2^31 with one multiply-high: q = (umulhi(n, m) + n) >> s,
 // s = ceil(log2 d), m = 2^32 (2^s - d) / d + 1 (round-up multiplier).
+// Powers of two (the common case: built per FFT stage of every tile) skip
+// the 64-bit division: m = 1, and umulhi(n, 1) = 0 leaves n >> s.
 struct FDiv {
   unsigned d, m, s;
-  __device__ __forceinline__ explicit FDiv(unsigned d_) : d(d_), s(0) {
-    while ((1u << s) < d) ++s;
-    m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  __device__ __forceinline__ explicit FDiv(unsigned d_) : d(d_) {
+    s = d > 1 ? 32 - __clz(d - 1) : 0;  // ceil(log2 d)
+    m = (d & (d - 1)) == 0
+            ? 1u
+            : (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
   }
   __device__ __forceinline__ unsigned div(unsigned n) const {
     return (__umulhi(n, m) + n) >> s;
@@ -352,10 +356,18 @@ struct FDiv {
 struct Walk {
   int b, j, tb, tj, len;
   __device__ __forceinline__ Walk(int f0, int len_, int T) : len(len_) {
-    b = f0 / len;
-    j = f0 - b * len;
-    tb = T / len;
-    tj = T - tb * len;
+    if (len > 0 && (len & (len - 1)) == 0) {  // shifts for powers of two
+      const int lg = __ffs(len) - 1;
+      b = f0 >> lg;
+      j = f0 & (len - 1);
+      tb = T >> lg;
+      tj = T & (len - 1);
+    } else {
+      b = f0 / len;
+      j = f0 - b * len;
+      tb = T / len;
+      tj = T - tb * len;
+    }
   }
   __device__ __forceinline__ void next() {
     j += tj;
@@ -463,7 +475,8 @@ __device__ __forceinline__ void fft_stage_body(C *sm, int Lp, int B, int Lf,
   const int total = B * nw;
   const FDiv dnw((unsigned)nw), dM((unsigned)M);
   const int lgB = __ffs(B) - 1;
-  const int tscale = Lf / Mprev;
+  const int tscale = (Mprev & (Mprev - 1)) == 0 ? Lf >> (__ffs(Mprev) - 1)
+                                                 : Lf / Mprev;
   for (int g = tid; g < total; g += T) {
     int b, w;
     if constexpr (LAY == 1) {
