@@ -1106,8 +1106,9 @@ __device__ __forceinline__ void issue_load(const Step &p, E *sm, unsigned bar,
     if (tid == 0)
       mbar_expect_tx(bar, (unsigned)((size_t)nv * p.in_len * sizeof(E)));
     const E *src = (const E *)p.src;
+    const FDiv dch((unsigned)nch);
     for (int c = tid; c < nv * nch; c += T) {
-      const int b = c / nch, k = c - b * nch;
+      const int b = (int)dch.div((unsigned)c), k = c - b * nch;
       const unsigned g = (unsigned)(gv0 + b);
       const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
       const i64 off = (i64)m * p.ld_src + (i64)v * p.vin.n + (i64)k * CH;
@@ -1149,8 +1150,9 @@ __device__ __forceinline__ void issue_store(const Step &p, const E *sm,
     E *dst = (E *)p.dst;
     fence_async_smem();
     bool any = false;
+    const FDiv dch((unsigned)nch);
     for (int c = tid; c < nv * nch; c += T) {
-      const int b = c / nch, k = c - b * nch;
+      const int b = (int)dch.div((unsigned)c), k = c - b * nch;
       const unsigned g = (unsigned)(gv0 + b);
       const unsigned m = dV.div(g), v = g - m * (unsigned)p.V;
       const i64 off = (i64)m * p.ld_dst + (i64)v * p.vout.n + (i64)k * CH;
