@@ -805,7 +805,13 @@ class _Solved(Matrix):
 
     def _transform(self, x, direction):
         if _is_tensor(x):
-            x = x.cpu().numpy()
+            # the solver iterates on the host; a tensor comes back as a
+            # (column-major) tensor on its device
+            y = self._transform(x.detach().cpu().numpy(), direction)
+            torch = _torch()
+            if y.ndim == 1:
+                return torch.from_numpy(y).to(x.device)
+            return torch.from_numpy(np.ascontiguousarray(y.T)).to(x.device).t()
         x = np.asarray(x)
         if x.ndim < 1 or x.ndim > 2:
             raise ValueError("Input data array must be 1D or 2D")

@@ -179,6 +179,11 @@ def test_inverse_and_pseudo_inverse():
     assert xh.shape == (n,)
     assert np.linalg.norm(d.conj().T @ xh - b[:, 0]) <= 1e-5 * np.linalg.norm(
         b[:, 0])
+    # a device tensor in, a device tensor out
+    import torch
+    xt = C.inverse.forward(torch.from_numpy(b).cuda())
+    assert xt.is_cuda and tuple(xt.shape) == (n, 2)
+    assert np.linalg.norm(d @ xt.cpu().numpy() - b) <= 1e-5 * np.linalg.norm(b)
     rows = np.sort(rng.choice(n, 30, replace=False))
     P = fg.Partial(C, rows=rows)
     y = P.pseudoInverse.forward(b[rows, 0])
