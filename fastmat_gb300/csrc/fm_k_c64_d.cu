@@ -10,6 +10,7 @@ KFn pick_c64_dense(int cls) {
     case 1: return vprog_kernel<float2, 1, 2>;
     case 2: return vprog_kernel<float2, 2, 2>;
     case 3: return vprog_kernel<float2, 3, 2>;
+    case 5: return vprog_kernel<float2, 5, 2>;
     default: return nullptr;
   }
 }

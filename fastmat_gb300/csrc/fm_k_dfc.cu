@@ -17,6 +17,8 @@ KFn pick_main(int cls, int lay) {
     case 9: return vprog_kernel<dfc, 3, 0>;
     case 4: return vprog_kernel<dfc, 1, 1>;
     case 10: return vprog_kernel<dfc, 3, 1>;
+    case 15: return vprog_kernel<dfc, 5, 0>;
+    case 16: return vprog_kernel<dfc, 5, 1>;
     default: return nullptr;
   }
 }

@@ -369,11 +369,11 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   // element-major tiles: strided input and output views whose inner extent
   // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
   // budget allows, never below 16 B), moved by TMA boxes
-  if (want_lay == 1 && !(allow_em && (ls.cls == 1 || ls.cls == 3 ||
-                                      ls.cls == 4)))
-    return false;
-  if (allow_em && (want_lay == -1 || want_lay == 1) &&
-      (ls.cls == 1 || ls.cls == 3 || ls.cls == 4) && st.vin.Cc > 1 &&
+  const bool em_class =
+      ls.cls == 1 || ls.cls == 3 || ls.cls == 4 || ls.cls == 5;
+  if (want_lay == 1 && !(allow_em && em_class)) return false;
+  if (allow_em && (want_lay == -1 || want_lay == 1) && em_class &&
+      st.vin.Cc > 1 &&
       st.vout.Cc > 1) {
     int B = want_B ? want_B : 128 / esz;
     if (!want_B) {
@@ -1420,6 +1420,21 @@ class Planner {
     return 3;
   }
 
+  // a forward (DIF) transform followed by a product with one table over
+  // the whole vector: kernel class 5 applies the product in the transform's
+  // last stage (its radix a power of two)
+  static bool spectrum_fusable(const std::vector<fmk::Op> &ops) {
+    for (size_t i = 0; i + 1 < ops.size(); ++i) {
+      const fmk::Op &a = ops[i], &m = ops[i + 1];
+      if (a.kind != fmk::OP_DIF || a.nrad < 1) continue;
+      const int last = a.rad[a.nrad - 1];
+      if (m.kind == fmk::OP_MUL && m.div == 1 && m.mod == 1 &&
+          m.len == a.len && last > 1 && (last & (last - 1)) == 0)
+        return true;
+    }
+    return false;
+  }
+
   // whether lowering the FFTs of a program to DIF/DIT needs an explicit
   // reordering gather (an order-sensitive op follows a digit-reversed FFT)
   static bool needs_gather(const std::vector<fmk::Op> &ops) {
@@ -1462,6 +1477,7 @@ class Planner {
     st.nops = (int)ops.size();
     for (size_t i = 0; i < ops.size(); ++i) st.ops[i] = ops[i];
     ls.cls = kernel_class(ops);
+    if (ls.cls == 1 && spectrum_fusable(ops)) ls.cls = 5;
     const bool odd = ls.cls == 2 || ls.cls == 0;
     ls.ept = odd ? ept_ / 2 : ept_;
     if (!configure(P_->esz, ls, 0, 0))
@@ -2653,7 +2669,9 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
         const i64 tiles = (st.V * M + st.B - 1) / st.B;
         if (st.V * M >= 0x7fffffffLL)
           fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
-        items.push_back(Item{level++, st, ls.cls, tiles});
+        // the batch kernel has no class 5: its class 1 runs the same
+        // program with the spectrum product as a separate op
+        items.push_back(Item{level++, st, ls.cls == 5 ? 1 : ls.cls, tiles});
       }
     }
     if (items.empty()) fail(FM_ERR_VALUE, "fm_batch_create: no work");

@@ -440,6 +440,14 @@ __device__ __forceinline__ void group_sync(int T) {
     __syncthreads();
 }
 
+// A pointwise product applied by the last stage of a forward transform as
+// it stores its outputs (the spectrum product of a circular convolution,
+// kernel class 5): output j is multiplied by p[j] (conj: by conj(p[j])).
+struct Post {
+  const void *p;
+  int conj;
+};
+
 // a * w (SG < 0) or a * conj(w) (SG > 0) for a butterfly value a in the
 // butterfly's computing type and a twiddle w (unnormalised products and
 // sums for double-float; the plain complex product otherwise)
@@ -468,7 +476,7 @@ template <int R, bool DIT, int LAY, int SG, bool UT, class C>
 __device__ __forceinline__ void fft_stage_body(C *sm, int Lp, int B, int Lf,
                                                int Mprev,
                                                const C *__restrict__ tw,
-                                               int tid, int T) {
+                                               int tid, int T, Post post) {
   constexpr int sign = SG;
   const int M = Mprev / R;
   const int nw = Lf / R;
@@ -516,6 +524,12 @@ __device__ __forceinline__ void fft_stage_body(C *sm, int Lp, int B, int Lf,
           if (brev<R>(i) != 0)  // folded by the unrolled loop
             y = cmul_lazy<sign>(y, twt[brev<R>(i) * tstep]);
         }
+        if constexpr (!DIT && UT) {
+          if (post.p) {
+            const C pw = ((const C *)post.p)[base + M * brev<R>(i)];
+            y = post.conj ? cmul_lazy<+1>(y, pw) : cmul_lazy<-1>(y, pw);
+          }
+        }
         vec[jx<C, LAY>(base + M * brev<R>(i), B)] = from_lazy(y);
       }
     } else {
@@ -546,15 +560,17 @@ template <int R, bool DIT, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
                                           int Mprev,
                                           const C *__restrict__ tw, int tid,
-                                          int T) {
+                                          int T, Post post) {
   if constexpr ((R & (R - 1)) == 0) {
     if (Mprev == R)
-      fft_stage_body<R, DIT, LAY, SG, true>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      fft_stage_body<R, DIT, LAY, SG, true>(sm, Lp, B, Lf, Mprev, tw, tid, T,
+                                            post);
     else
       fft_stage_body<R, DIT, LAY, SG, false>(sm, Lp, B, Lf, Mprev, tw, tid,
-                                             T);
+                                             T, post);
   } else {
-    fft_stage_body<R, DIT, LAY, SG, false>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+    fft_stage_body<R, DIT, LAY, SG, false>(sm, Lp, B, Lf, Mprev, tw, tid, T,
+                                           post);
   }
   group_sync(T);
 }
@@ -580,27 +596,27 @@ template <class C> struct Radix16 {
 template <bool DIT, int CLS, int LAY, int SG, class C>
 __device__ __forceinline__ void fft_stage_s(int R, C *sm, int Lp, int B,
                                             int Lf, int Mprev, const C *tw,
-                                            int tid, int T) {
+                                            int tid, int T, Post post) {
   switch (R) {
-    case 2: fft_stage<2, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
-    case 4: fft_stage<4, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
-    case 8: fft_stage<8, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T); break;
+    case 2: fft_stage<2, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post); break;
+    case 4: fft_stage<4, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post); break;
+    case 8: fft_stage<8, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post); break;
     case 16:
       // double-float vectors of 16 elements do not fit the register budget
       if constexpr (Radix16<C>::v)
-        fft_stage<16, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+        fft_stage<16, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post);
       break;
     case 3:
-      if constexpr (CLS != 1)
-        fft_stage<3, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      if constexpr (CLS != 1 && CLS != 5)
+        fft_stage<3, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post);
       break;
     case 5:
-      if constexpr (CLS != 1)
-        fft_stage<5, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      if constexpr (CLS != 1 && CLS != 5)
+        fft_stage<5, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post);
       break;
     case 7:
-      if constexpr (CLS != 1)
-        fft_stage<7, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T);
+      if constexpr (CLS != 1 && CLS != 5)
+        fft_stage<7, DIT, LAY, SG>(sm, Lp, B, Lf, Mprev, tw, tid, T, post);
       break;
     default: break;
   }
@@ -611,22 +627,29 @@ __device__ __forceinline__ void fft_stage_s(int R, C *sm, int Lp, int B,
 template <bool DIT, int CLS, int LAY, class C>
 __device__ __forceinline__ void fft_stage_r(int R, C *sm, int Lp, int B,
                                             int Lf, int Mprev, int sign,
-                                            const C *tw, int tid, int T) {
+                                            const C *tw, int tid, int T,
+                                            Post post) {
   if (sign < 0)
-    fft_stage_s<DIT, CLS, LAY, -1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T);
+    fft_stage_s<DIT, CLS, LAY, -1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T, post);
   else
-    fft_stage_s<DIT, CLS, LAY, +1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T);
+    fft_stage_s<DIT, CLS, LAY, +1>(R, sm, Lp, B, Lf, Mprev, tw, tid, T, post);
 }
 
+// post: a pointwise product for the last DIF stage (class 5 only; its radix
+// is a power of two), otherwise none
 template <class C, int CLS, int LAY>
-__device__ void run_fft(const Op &op, C *sm, int Lp, int B, int tid, int T) {
+__device__ void run_fft(const Op &op, C *sm, int Lp, int B, int tid, int T,
+                        Post post) {
   const C *tw = (const C *)op.ptr;
   if (op.kind == OP_DIF) {
     int Mprev = op.len;
     for (int p = 0; p < op.nrad; ++p) {
       const int R = op.rad[p];
+      Post pp = Post{nullptr, 0};
+      if constexpr (CLS == 5)
+        if (p + 1 == op.nrad) pp = post;
       fft_stage_r<false, CLS, LAY>(R, sm, Lp, B, op.len, Mprev, op.sign, tw,
-                                   tid, T);
+                                   tid, T, pp);
       Mprev /= R;
     }
   } else {
@@ -634,7 +657,7 @@ __device__ void run_fft(const Op &op, C *sm, int Lp, int B, int tid, int T) {
     for (int p = op.nrad - 1; p >= 0; --p) {
       Mprev *= op.rad[p];
       fft_stage_r<true, CLS, LAY>(op.rad[p], sm, Lp, B, op.len, Mprev,
-                                  op.sign, tw, tid, T);
+                                  op.sign, tw, tid, T, Post{nullptr, 0});
     }
   }
 }
@@ -1490,8 +1513,23 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
     switch (op.kind) {
       case OP_DIF:
       case OP_DIT:
-        if constexpr (Tr<E>::cplx && CLS != 3)
-          run_fft<E, CLS, LAY>(op, sm, Lp, B, tid, T);
+        if constexpr (Tr<E>::cplx && CLS == 5) {
+          // a whole-vector product with one table right after a forward
+          // transform (a convolution's spectrum) is applied by the
+          // transform's last stage as it stores its outputs
+          const Op *nx = o + 1 < p.nops ? &p.ops[o + 1] : nullptr;
+          const int last = op.nrad > 0 ? op.rad[op.nrad - 1] : 0;
+          const bool fuse = op.kind == OP_DIF && nx && nx->kind == OP_MUL &&
+                            nx->div == 1 && nx->mod == 1 &&
+                            nx->len == op.len && last > 1 &&
+                            (last & (last - 1)) == 0;
+          run_fft<E, CLS, LAY>(op, sm, Lp, B, tid, T,
+                               fuse ? Post{nx->ptr, nx->sign}
+                                    : Post{nullptr, 0});
+          if (fuse) ++o;
+        } else if constexpr (Tr<E>::cplx && CLS != 3) {
+          run_fft<E, CLS, LAY>(op, sm, Lp, B, tid, T, Post{nullptr, 0});
+        }
         break;
       case OP_FWHT:
         if constexpr (CLS == 0 || CLS == 3 || CLS == 4)
@@ -1521,7 +1559,9 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // programs (power-of-two FFT, FWHT) do not carry the register pressure of
 // the rarely used ops: 1 = pow2 FFT + pointwise, 2 = FFT with radices 3/5/7,
 // 3 = FWHT + pointwise, 4 = FWHT with 16-point groups on the tensor cores
-// (float only) + pointwise, 0 = everything.  LAY is the tile layout.
+// (float only) + pointwise, 5 = as 1 with a convolution's spectrum product
+// applied by the last stage of the forward transform, 0 = everything.  LAY
+// is the tile layout.
 //
 // Persistent CTAs: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x,
 // ...  Tiles are copied into a ring of p.nbuf shared-memory buffers
