@@ -115,6 +115,28 @@ def test_c_abi_library_exports_every_declared_symbol():
     assert lib.fm_version() >= 100
 
 
+def test_constants_match_header():
+    """Node kinds, element / compute types, directions and status codes of
+    the Python binding equal the header's #defines."""
+    with open(os.path.join(ROOT, 'include', 'fmgpu.h')) as f:
+        defs = dict((k, int(v)) for k, v in re.findall(
+            r'#define\s+(FM_[A-Z0-9_]+)\s+(-?\d+)\b', f.read()))
+    nodes = {k[len('FM_NODE_'):]: v for k, v in defs.items()
+             if k.startswith('FM_NODE_')}
+    assert len(nodes) == 16
+    for name, v in nodes.items():
+        assert getattr(_native, 'NODE_' + name) == v, name
+    for name in ('FM_F32_TC', 'FM_F64_DF', 'FM_C128_DF'):
+        assert getattr(_native, name) == defs[name], name
+    assert (_native.FORWARD, _native.BACKWARD) == (defs['FM_FORWARD'],
+                                                  defs['FM_BACKWARD'])
+    for dt, name in ((np.int8, 'FM_I8'), (np.int16, 'FM_I16'),
+                     (np.int32, 'FM_I32'), (np.int64, 'FM_I64'),
+                     (np.float32, 'FM_F32'), (np.float64, 'FM_F64'),
+                     (np.complex64, 'FM_C64'), (np.complex128, 'FM_C128')):
+        assert _native.DTYPE_CODE[np.dtype(dt)] == defs[name], name
+
+
 def test_node_struct_layout_matches_header(tmp_path):
     """The ctypes mirrors of fm_node / fm_plan_info have the C layout."""
     import ctypes
