@@ -191,3 +191,51 @@ def test_block_constructors_validate_like_fastmat():
     D = fg.BlockDiag(F3, H2, fg.Diag(np.arange(2.0)))
     assert D.shape == (9, 9) and D.dtype == np.complex128
     assert fg.BlockDiag(H2, fg.Eye(2)).dtype == np.int8
+
+
+def test_accessor_and_solver_argument_errors():
+    """Argument checks of the dense accessors, Sparse and the solver-backed
+    operators raise before any device work (fastmat/Matrix.pyx:389-658,
+    2490-2600; fastmat/Sparse.pyx:95-115)."""
+    c = np.arange(1.0, 13.0)
+    P = fg.Partial(fg.Circulant(c), rows=np.array([0, 3, 4, 7, 11]))
+    with pytest.raises(IndexError):
+        P.getCol(12)
+    with pytest.raises(IndexError):
+        P.getRow(-1)
+    with pytest.raises(IndexError):
+        P.getCols([0, 12])
+    with pytest.raises(IndexError):
+        P.getRows(np.array([[0, 1]]))
+    with pytest.raises(TypeError):
+        P.getCol([1, 2])
+    with pytest.raises(IndexError):
+        P[1, 2, 3]
+    with pytest.raises(IndexError):
+        P[()]
+    with pytest.raises(IndexError):
+        P[1]
+    with pytest.raises(TypeError):
+        P[[0.5, 1.0], :]
+    with pytest.raises(TypeError):
+        P[{1: 2}, 0]
+    with pytest.raises(TypeError):
+        fg.Sparse(np.eye(3))
+    with pytest.raises(TypeError):
+        fg.Sparse([[1, 0], [0, 1]])
+    with pytest.raises(ValueError):
+        fg.Inverse(P)
+    with pytest.raises(TypeError):
+        fg.Inverse(np.eye(3))
+    with pytest.raises(TypeError):
+        fg.PseudoInverse(np.eye(3))
+    C = fg.Circulant(c)
+    assert C.inverse.shape == (12, 12) and C.pseudoInverse.shape == (12, 12)
+    assert P.pseudoInverse.shape == (12, 5)
+    with pytest.raises(NotImplementedError):
+        fg.Product(C.inverse, C).forward(np.ones(12))
+    wide = fg.Partial(fg.Fourier(4), rows=np.array([0, 1]))
+    with pytest.raises(ValueError):
+        wide.largestEigenValue
+    with pytest.raises(ValueError):
+        wide.largestEigenVec
