@@ -72,13 +72,15 @@ class FmPlanInfo(ctypes.Structure):
 
 #: every entry point include/fmgpu.h declares
 EXPORTS = ('fm_plan_create', 'fm_execute', 'fm_execute_profiled',
-           'fm_execute_static', 'fm_execute_host', 'fm_plan_check',
+           'fm_execute_static', 'fm_execute_host', 'fm_release_host_staging',
+           'fm_plan_check',
            'fm_plan_set_tile', 'fm_plan_set_tile_layout', 'fm_plan_get_tile',
-           'fm_plan_autotune',
+           'fm_plan_autotune', 'fm_plan_set_wait_limit',
            'fm_plan_destroy', 'fm_plan_get_info', 'fm_plan_describe',
            'fm_batch_create', 'fm_batch_execute', 'fm_batch_execute_graph',
-           'fm_batch_check', 'fm_batch_get_info', 'fm_batch_destroy',
-           'fm_reduce_mulconj', 'fm_last_error', 'fm_version')
+           'fm_batch_check', 'fm_batch_set_wait_limit', 'fm_batch_get_info',
+           'fm_batch_destroy', 'fm_reduce_mulconj',
+           'fm_debug_fail_allocation', 'fm_last_error', 'fm_version')
 
 _lib = None
 _lock = threading.Lock()
@@ -132,6 +134,14 @@ def load(build_if_missing=True):
         lib.fm_plan_autotune.restype = ctypes.c_int
         lib.fm_plan_check.argtypes = [P]
         lib.fm_plan_check.restype = ctypes.c_int
+        lib.fm_plan_set_wait_limit.argtypes = [P, I64]
+        lib.fm_plan_set_wait_limit.restype = ctypes.c_int
+        lib.fm_batch_set_wait_limit.argtypes = [P, I64]
+        lib.fm_batch_set_wait_limit.restype = ctypes.c_int
+        lib.fm_release_host_staging.argtypes = []
+        lib.fm_release_host_staging.restype = ctypes.c_int
+        lib.fm_debug_fail_allocation.argtypes = [I32]
+        lib.fm_debug_fail_allocation.restype = ctypes.c_int
         lib.fm_plan_destroy.argtypes = [P]
         lib.fm_plan_destroy.restype = ctypes.c_int
         lib.fm_plan_get_info.argtypes = [P, ctypes.POINTER(FmPlanInfo)]
@@ -254,6 +264,11 @@ class Plan:
         """Raise if a kernel of this plan reported a failure (syncs)."""
         check(self._lib.fm_plan_check(self.handle))
 
+    def set_wait_limit(self, polls):
+        """Polls of a bounded device wait before it gives up (see
+        fm_plan_set_wait_limit; default 2^22)."""
+        check(self._lib.fm_plan_set_wait_limit(self.handle, polls))
+
     def info(self):
         inf = FmPlanInfo()
         check(self._lib.fm_plan_get_info(self.handle, ctypes.byref(inf)))
@@ -273,6 +288,18 @@ class Plan:
             except Exception:
                 pass
             self.handle = None
+
+
+def release_host_staging():
+    """Free the device buffers the host entry point keeps for the current
+    device (fm_release_host_staging)."""
+    check(load().fm_release_host_staging())
+
+
+def fail_allocation(after):
+    """Test hook: make the device allocation after `after` more successful
+    ones fail (fm_debug_fail_allocation); after < 0 disarms."""
+    check(load().fm_debug_fail_allocation(after))
 
 
 def reduce_mulconj(A, n, Cc, num_cols, type_code, u, ld_u, v, ld_v, out,
@@ -311,6 +338,10 @@ class BatchHandle:
 
     def check(self):
         check(self._lib.fm_batch_check(self.handle))
+
+    def set_wait_limit(self, polls):
+        """Polls of a grid-barrier wait (fm_batch_set_wait_limit)."""
+        check(self._lib.fm_batch_set_wait_limit(self.handle, polls))
 
     def info(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -93,6 +93,12 @@ class Batch:
         """Synchronise and raise if a bounded wait of the launch gave up."""
         self._h.check()
 
+    def set_wait_limit(self, polls):
+        """Polls of a grid-barrier wait before the launch gives up and
+        reports a timeout (default 2^22; 0: at once).  Set it before the
+        first ``run(graph=True)``."""
+        self._h.set_wait_limit(polls)
+
     def info(self):
         """(launches of the separate plans, levels, tiles)."""
         return self._h.info()

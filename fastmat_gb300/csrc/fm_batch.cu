@@ -40,7 +40,7 @@ cudaError_t launch_one(const BatchLaunch &b, cudaStream_t s) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, fn, b.steps, b.start, b.level, b.nlev,
-                            b.bar, b.err, b.max_B, b.max_tile);
+                            b.bar, b.err, b.max_B, b.max_tile, b.wait_limit);
 }
 
 }  // namespace

@@ -37,6 +37,7 @@ struct BatchLaunch {
   size_t max_tile = 0;  // bytes of the largest tile (one of two slots)
   size_t smem = 0;
   long long max_level_tiles = 1;
+  long long wait_limit = 1LL << 22;  // polls of a grid-barrier wait
 };
 cudaError_t launch_batch(const BatchLaunch &b, cudaStream_t s);
 

@@ -19,6 +19,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -51,6 +52,36 @@ struct Error {
       fail(e_ == cudaErrorMemoryAllocation ? FM_ERR_NOMEM : FM_ERR_CUDA,    \
            std::string(#x) + ": " + cudaGetErrorString(e_));                \
   } while (0)
+
+// One-shot allocation failure for tests of the out-of-memory path
+// (fm_debug_fail_allocation): after g_alloc_skip more successful device
+// allocations the next one fails as if the device were full; -1 = disarmed.
+std::atomic<long long> g_alloc_skip{-1};
+
+template <class T> cudaError_t dev_malloc(T **p, size_t bytes) {
+  long long k = g_alloc_skip.load();
+  while (k >= 0) {
+    if (g_alloc_skip.compare_exchange_weak(k, k - 1)) {
+      if (k == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMalloc((void **)p, bytes);
+}
+
+// a device buffer freed when it goes out of scope (planner temporaries)
+struct DevTemp {
+  void *p = nullptr;
+  DevTemp() = default;
+  DevTemp(const DevTemp &) = delete;
+  DevTemp &operator=(const DevTemp &) = delete;
+  ~DevTemp() {
+    if (p) cudaFree(p);
+  }
+};
 
 int esize(int t) {
   switch (t) {
@@ -234,25 +265,14 @@ struct fm_plan {
   // execution state
   void *scratch = nullptr;
   size_t scratch_cap = 0;
-  // host execution staging
-  void *dx = nullptr, *dy = nullptr;
-  size_t dx_cap = 0, dy_cap = 0;
-  cudaStream_t hstream = nullptr;          // compute
-  cudaStream_t hin = nullptr, hout = nullptr;  // copies in / out
-  std::vector<cudaEvent_t> hev;          // chunk hand-over events
   int *err = nullptr;  // device status word written by bounded waits
+  long long wait_limit = FM_WAIT_LIMIT;  // polls of a bounded copy wait
   ~fm_plan();
 };
 
 fm_plan::~fm_plan() {
   for (void *p : allocs) cudaFree(p);
   if (scratch) cudaFree(scratch);
-  if (dx) cudaFree(dx);
-  if (dy) cudaFree(dy);
-  if (hstream) cudaStreamDestroy(hstream);
-  if (hin) cudaStreamDestroy(hin);
-  if (hout) cudaStreamDestroy(hout);
-  for (cudaEvent_t e : hev) cudaEventDestroy(e);
 }
 
 struct fm_batch {
@@ -502,7 +522,7 @@ class Planner {
   // ---------------------------------------------------------- device data
   void *dalloc(size_t bytes) {
     void *p = nullptr;
-    CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    CUDA_TRY(dev_malloc(&p, std::max<size_t>(bytes, 16)));
     P_->allocs.push_back(p);
     P_->const_bytes += (i64)bytes;
     return p;
@@ -619,16 +639,14 @@ class Planner {
   // optionally in the four-step (L1, L2) layout
   const void *spectrum(const std::vector<cd> &v, i64 L1 = 0, i64 L2 = 0) {
     const i64 L = (i64)v.size();
-    double2 *din = nullptr, *dout = nullptr;
-    CUDA_TRY(cudaMalloc(&din, L * sizeof(double2)));
-    CUDA_TRY(cudaMalloc(&dout, L * sizeof(double2)));
+    DevTemp tin, tout;
+    CUDA_TRY(dev_malloc(&tin.p, L * sizeof(double2)));
+    CUDA_TRY(dev_malloc(&tout.p, L * sizeof(double2)));
+    double2 *din = (double2 *)tin.p, *dout = (double2 *)tout.p;
     CUDA_TRY(cudaMemcpy(din, v.data(), L * sizeof(double2),
                         cudaMemcpyHostToDevice));
     fft_f64_device(din, dout, L);
-    const void *res = convert_dev(dout, L, 1.0 / (double)L, L1, L2);
-    cudaFree(din);
-    cudaFree(dout);
-    return res;
+    return convert_dev(dout, L, 1.0 / (double)L, L1, L2);
   }
 
   const void *convert_dev(const double2 *src, i64 n, double scale, i64 L1,
@@ -1011,9 +1029,10 @@ class Planner {
     }
     // Bluestein: x -> a . x -> (*) h -> a . (first N)
     const i64 Lb = next_pow2(2 * N - 1);
-    double2 *da = nullptr, *dh = nullptr;
-    CUDA_TRY(cudaMalloc(&da, N * sizeof(double2)));
-    CUDA_TRY(cudaMalloc(&dh, Lb * sizeof(double2)));
+    DevTemp ta, th;
+    CUDA_TRY(dev_malloc(&ta.p, N * sizeof(double2)));
+    CUDA_TRY(dev_malloc(&th.p, Lb * sizeof(double2)));
+    double2 *da = (double2 *)ta.p, *dh = (double2 *)th.p;
     k_chirp<<<grid_for(N), 256>>>(da, N);
     k_bluestein_filter<<<grid_for(Lb), 256>>>(dh, da, N, Lb);
     CUDA_TRY(cudaGetLastError());
@@ -1022,8 +1041,6 @@ class Planner {
     std::vector<double2> hh((size_t)Lb);
     CUDA_TRY(cudaMemcpy(hh.data(), dh, Lb * sizeof(double2),
                         cudaMemcpyDeviceToHost));
-    cudaFree(da);
-    cudaFree(dh);
     std::vector<cd> filt((size_t)Lb);
     for (i64 i = 0; i < Lb; ++i) filt[i] = cd(hh[i].x, hh[i].y);
     return conv(Lb, N, N, filt, false, chirp, chirp, !fwd);
@@ -1077,21 +1094,25 @@ class Planner {
         Unit u;
         u.kind = Unit::STEPS;
         u.n_in = u.n_out = N;
-        SStep a;
-        a.vin = a.vout = fmk::View{1, N1, N2};
-        a.in_rows = a.out_rows = N;
-        a.L = a.in_len = a.out_len = (int)N1;
-        a.src = -1;
-        a.dst = -2;
-        a.ops.push_back(fwht_op(N1));
+        // the low index bits first (contiguous vectors of N2), then the
+        // high bits (vectors of N1 at stride N2): the butterflies then run
+        // in fastmat's order, distance 1, 2, 4, ... (fastmat/Hadamard.pyx:
+        // 182-228), so single-precision results are bit-identical to it
         SStep b;
         b.vin = b.vout = fmk::View{N1, N2, 1};
         b.in_rows = b.out_rows = N;
         b.L = b.in_len = b.out_len = (int)N2;
-        b.src = -2;
+        b.src = -1;
         b.dst = -2;
         b.ops.push_back(fwht_op(N2));
-        u.steps = {a, b};
+        SStep a;
+        a.vin = a.vout = fmk::View{1, N1, N2};
+        a.in_rows = a.out_rows = N;
+        a.L = a.in_len = a.out_len = (int)N1;
+        a.src = -2;
+        a.dst = -2;
+        a.ops.push_back(fwht_op(N1));
+        u.steps = {b, a};
         c.push_back(u);
         return c;
       }
@@ -1901,6 +1922,7 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
     return;
   }
   st.err = P->err;
+  st.wait_limit = P->wait_limit;
   st.tma_in = st.tma_out = 0;
   if (ls.lay == 0 || ls.lay == 2) {
     const int esz = P->esz;
@@ -1986,7 +2008,7 @@ int run_plan(fm_plan *P, int dir, const void *x, int x_type, i64 ld_x,
       P->scratch = nullptr;
       P->scratch_cap = 0;
     }
-    CUDA_TRY(cudaMalloc(&P->scratch, total));
+    CUDA_TRY(dev_malloc(&P->scratch, total));
     P->scratch_cap = total;
   }
   size_t li = 0;
@@ -2113,6 +2135,41 @@ const char *kind_name(int k) {
   return "?";
 }
 
+// Whether the subtree at `id` only moves data: gathers, scatters, zero
+// fills and conjugation (Permutation, Partial, Eye, Hermitian, Conjugate),
+// scalars +-1 / +-i, and Sum / Kron / Blocks / Product of such subtrees.
+// Such trees run in the I/O element type itself rather than double-float, so
+// every output element is an input element (or an IEEE sum of them, in
+// fastmat's order for Sum), bit for bit as in fastmat's gathers
+// (fastmat/Permutation.pyx:120-124, fastmat/Partial.pyx:268-294).
+bool moves_data_only(const std::vector<NodeRec> &recs, int id, int depth = 0) {
+  if (id < 0) return true;  // zero block of a Blocks node
+  if (depth > 256 || id >= (int)recs.size()) return false;
+  const NodeRec &r = recs[(size_t)id];
+  auto children = [&]() {
+    for (int c : r.ch)
+      if (!moves_data_only(recs, c, depth + 1)) return false;
+    return true;
+  };
+  switch (r.d.kind) {
+    case FM_NODE_PERMUTATION:
+    case FM_NODE_EYE: return true;
+    case FM_NODE_PARTIAL:
+    case FM_NODE_HERMITIAN:
+    case FM_NODE_CONJUGATE:
+    case FM_NODE_SUM:
+    case FM_NODE_KRON:
+    case FM_NODE_BLOCKS: return children();
+    case FM_NODE_PRODUCT: {
+      const double re = r.d.scalar_re, im = r.d.scalar_im;
+      const bool unit = (im == 0.0 && (re == 1.0 || re == -1.0)) ||
+                        (re == 0.0 && (im == 1.0 || im == -1.0));
+      return unit && children();
+    }
+    default: return false;
+  }
+}
+
 template <class F> int guarded(F f) {
   try {
     g_err.clear();
@@ -2127,6 +2184,84 @@ template <class F> int guarded(F f) {
     g_err = e.what();
     return FM_ERR_VALUE;
   }
+}
+
+void check_device(int want, const char *what) {
+  int dev = -1;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != want)
+    fail(FM_ERR_VALUE, std::string(what) + " was built on device " +
+                           std::to_string(want) + " but device " +
+                           std::to_string(dev) + " is current");
+}
+
+// Arguments common to the execute entry points; the plan must run on the
+// device it was built on (its constants and scratch live there).
+void check_call(const fm_plan *plan, int direction, const void *x, int x_type,
+                i64 ld_x, const void *y, int y_type, i64 ld_y, i64 num_cols) {
+  if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+  if (direction != FM_FORWARD && direction != FM_BACKWARD)
+    fail(FM_ERR_VALUE, "invalid direction");
+  if (!valid_type(x_type) || !valid_type(y_type))
+    fail(FM_ERR_TYPE, "unsupported element type");
+  const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
+  const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
+  if (num_cols < 0) fail(FM_ERR_VALUE, "negative column count");
+  if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "NULL data pointer");
+  if (ld_x < n_in || ld_y < n_out)
+    fail(FM_ERR_VALUE, "leading dimension smaller than the vector size");
+  check_device(plan->device, "the plan");
+}
+
+// Report and clear a failure kernels of the plan recorded on the device.
+int check_status(fm_plan *plan) {
+  if (!plan->err) return FM_OK;
+  int e = 0;
+  CUDA_TRY(cudaMemcpy(&e, plan->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e != 0) {
+    CUDA_TRY(cudaMemset(plan->err, 0, sizeof(int)));
+    fail(FM_ERR_TIMEOUT,
+         "a bounded wait for a tile copy gave up; results of the affected "
+         "call are incomplete");
+  }
+  return FM_OK;
+}
+
+// Device staging of fm_execute_host, one per device and shared by every
+// plan (calls on one device take turns): the operand buffers, sized by the
+// largest call so far, and the copy-in / compute / copy-out streams.  Kept
+// until the process exits.
+struct HostStage {
+  std::mutex mu;
+  void *dx = nullptr, *dy = nullptr;
+  size_t dx_cap = 0, dy_cap = 0;
+  cudaStream_t comp = nullptr, in = nullptr, out = nullptr;
+  std::vector<cudaEvent_t> ev;  // chunk hand-over events
+  void reserve(size_t bx, size_t by) {
+    if (bx > dx_cap) {
+      if (dx) cudaFree(dx);
+      dx = nullptr;
+      dx_cap = 0;
+      CUDA_TRY(dev_malloc(&dx, bx));
+      dx_cap = bx;
+    }
+    if (by > dy_cap) {
+      if (dy) cudaFree(dy);
+      dy = nullptr;
+      dy_cap = 0;
+      CUDA_TRY(dev_malloc(&dy, by));
+      dy_cap = by;
+    }
+  }
+};
+
+HostStage &host_stage(int dev) {
+  static std::mutex mu;
+  static std::map<int, HostStage *> stages;
+  std::lock_guard<std::mutex> lock(mu);
+  HostStage *&h = stages[dev];
+  if (!h) h = new HostStage();
+  return *h;
 }
 
 }  // namespace
@@ -2169,15 +2304,20 @@ int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
       }
       if (d.rows < 0 || d.cols < 0) fail(FM_ERR_VALUE, "negative shape");
     }
+    // data movement computes in the buffers' own type: bit-exact
+    int ctype = compute_type;
+    if ((ctype == FM_F64_DF || ctype == FM_C128_DF || ctype == FM_F32_TC) &&
+        moves_data_only(recs, root))
+      ctype = io_of(ctype);
     std::unique_ptr<fm_plan> P(new fm_plan);
-    P->ctype = compute_type;
-    P->io_type = io_of(compute_type);
-    P->esz = esize(compute_type);
+    P->ctype = ctype;
+    P->io_type = io_of(ctype);
+    P->esz = esize(ctype);
     CUDA_TRY(cudaGetDevice(&P->device));
     P->rows = nodes[root].rows;
     P->cols = nodes[root].cols;
     Planner(P.get(), recs).build(root);
-    CUDA_TRY(cudaMalloc(&P->err, sizeof(int)));
+    CUDA_TRY(dev_malloc(&P->err, sizeof(int)));
     P->allocs.push_back(P->err);
     CUDA_TRY(cudaMemset(P->err, 0, sizeof(int)));
     CUDA_TRY(cudaDeviceSynchronize());
@@ -2190,17 +2330,7 @@ int fm_execute(fm_plan *plan, int32_t direction, const void *x, int32_t x_type,
                int64_t ld_x, void *y, int32_t y_type, int64_t ld_y,
                int64_t num_cols, void *stream) {
   return guarded([&]() {
-    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
-    if (direction != FM_FORWARD && direction != FM_BACKWARD)
-      fail(FM_ERR_VALUE, "invalid direction");
-    if (!valid_type(x_type) || !valid_type(y_type))
-      fail(FM_ERR_TYPE, "unsupported element type");
-    const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
-    const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
-    if (num_cols < 0) fail(FM_ERR_VALUE, "negative column count");
-    if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "NULL data pointer");
-    if (ld_x < n_in || ld_y < n_out)
-      fail(FM_ERR_VALUE, "leading dimension smaller than the vector size");
+    check_call(plan, direction, x, x_type, ld_x, y, y_type, ld_y, num_cols);
     return run_plan(plan, direction, x, x_type, ld_x, y, y_type, ld_y,
                     num_cols, (cudaStream_t)stream);
   });
@@ -2211,11 +2341,8 @@ int fm_execute_profiled(fm_plan *plan, int32_t direction, const void *x,
                         int64_t ld_y, int64_t num_cols, void *stream,
                         float *ms, int32_t *num_launches) {
   return guarded([&]() {
-    if (!plan || !ms || !num_launches) fail(FM_ERR_VALUE, "NULL argument");
-    if (direction != FM_FORWARD && direction != FM_BACKWARD)
-      fail(FM_ERR_VALUE, "invalid direction");
-    if (!valid_type(x_type) || !valid_type(y_type))
-      fail(FM_ERR_TYPE, "unsupported element type");
+    if (!ms || !num_launches) fail(FM_ERR_VALUE, "NULL argument");
+    check_call(plan, direction, x, x_type, ld_x, y, y_type, ld_y, num_cols);
     const size_t n = plan->steps[direction].size();
     if ((size_t)*num_launches < n) fail(FM_ERR_VALUE, "ms array too short");
     std::vector<cudaEvent_t> ev(n + 1, nullptr);
@@ -2244,17 +2371,7 @@ int fm_execute_static(fm_plan *plan, int32_t direction, const void *x,
                       int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
                       int64_t ld_y, int64_t num_cols, void *stream) {
   return guarded([&]() {
-    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
-    if (direction != FM_FORWARD && direction != FM_BACKWARD)
-      fail(FM_ERR_VALUE, "invalid direction");
-    if (!valid_type(x_type) || !valid_type(y_type))
-      fail(FM_ERR_TYPE, "unsupported element type");
-    const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
-    const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
-    if (num_cols < 0) fail(FM_ERR_VALUE, "negative column count");
-    if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "NULL data pointer");
-    if (ld_x < n_in || ld_y < n_out)
-      fail(FM_ERR_VALUE, "leading dimension smaller than the vector size");
+    check_call(plan, direction, x, x_type, ld_x, y, y_type, ld_y, num_cols);
     return run_plan_static(plan, direction, x, x_type, ld_x, y, y_type, ld_y,
                            num_cols, (cudaStream_t)stream);
   });
@@ -2263,73 +2380,68 @@ int fm_execute_static(fm_plan *plan, int32_t direction, const void *x,
 int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
                     int32_t x_type, int64_t ld_x, void *y, int32_t y_type,
                     int64_t ld_y, int64_t num_cols) {
-  // streams that may still hold copies into the caller's buffers are
-  // drained before any return
-  auto drain = [&]() {
-    if (!plan) return;
-    for (cudaStream_t st : {plan->hin, plan->hstream, plan->hout})
-      if (st) cudaStreamSynchronize(st);
-  };
+  if (!plan) return guarded([]() -> int { fail(FM_ERR_VALUE, "plan is NULL"); });
+  // the call runs on the plan's device and leaves the caller's current
+  // device as it was
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  const bool switched = prev != plan->device;
+  if (switched && cudaSetDevice(plan->device) != cudaSuccess)
+    return guarded([&]() -> int {
+      fail(FM_ERR_CUDA, "cannot make the plan's device current");
+    });
+  HostStage &hs = host_stage(plan->device);
+  std::lock_guard<std::mutex> lock(hs.mu);
   const int st = guarded([&]() {
-    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
-    if (!valid_type(x_type) || !valid_type(y_type))
-      fail(FM_ERR_TYPE, "unsupported element type");
+    if (num_cols > 0 && (!x || !y)) fail(FM_ERR_VALUE, "x or y is NULL");
+    check_call(plan, direction, x, x_type, ld_x, y, y_type, ld_y, num_cols);
     if (num_cols <= 0) return FM_OK;
-    if (!x || !y) fail(FM_ERR_VALUE, "x or y is NULL");
     const size_t cx = (size_t)ld_x * esize(x_type);  // bytes per column
     const size_t cy = (size_t)ld_y * esize(y_type);
     const size_t bx = cx * (size_t)num_cols, by = cy * (size_t)num_cols;
-    for (cudaStream_t *st : {&plan->hstream, &plan->hin, &plan->hout})
-      if (!*st) CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
-    if (bx > plan->dx_cap) {
-      if (plan->dx) cudaFree(plan->dx);
-      plan->dx = nullptr;
-      plan->dx_cap = 0;
-      CUDA_TRY(cudaMalloc(&plan->dx, bx));
-      plan->dx_cap = bx;
-    }
-    if (by > plan->dy_cap) {
-      if (plan->dy) cudaFree(plan->dy);
-      plan->dy = nullptr;
-      plan->dy_cap = 0;
-      CUDA_TRY(cudaMalloc(&plan->dy, by));
-      plan->dy_cap = by;
-    }
+    for (cudaStream_t *sp : {&hs.comp, &hs.in, &hs.out})
+      if (!*sp) CUDA_TRY(cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking));
+    hs.reserve(bx, by);
     // column chunks of at least ~64 MiB of operands, at most 8
     const i64 want = (i64)std::min<size_t>(
         8, std::max<size_t>(1, (bx + by) / ((size_t)64 << 20)));
     const i64 per = (num_cols + std::min<i64>(want, num_cols) - 1) /
                     std::min<i64>(want, num_cols);
     const i64 nch = (num_cols + per - 1) / per;
-    while ((i64)plan->hev.size() < 2 * nch) {
+    while ((i64)hs.ev.size() < 2 * nch) {
       cudaEvent_t e;
       CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      plan->hev.push_back(e);
+      hs.ev.push_back(e);
     }
     for (i64 k = 0; k < nch; ++k) {
       const i64 c0 = k * per, m = std::min(per, num_cols - c0);
-      cudaEvent_t ev_in = plan->hev[(size_t)(2 * k)];
-      cudaEvent_t ev_done = plan->hev[(size_t)(2 * k + 1)];
-      char *dxk = (char *)plan->dx + c0 * cx;
-      char *dyk = (char *)plan->dy + c0 * cy;
+      cudaEvent_t ev_in = hs.ev[(size_t)(2 * k)];
+      cudaEvent_t ev_done = hs.ev[(size_t)(2 * k + 1)];
+      char *dxk = (char *)hs.dx + c0 * cx;
+      char *dyk = (char *)hs.dy + c0 * cy;
       CUDA_TRY(cudaMemcpyAsync(dxk, (const char *)x + c0 * cx, m * cx,
-                               cudaMemcpyHostToDevice, plan->hin));
-      CUDA_TRY(cudaEventRecord(ev_in, plan->hin));
-      CUDA_TRY(cudaStreamWaitEvent(plan->hstream, ev_in, 0));
-      const int s2 = fm_execute(plan, direction, dxk, x_type, ld_x, dyk,
-                                y_type, ld_y, m, plan->hstream);
+                               cudaMemcpyHostToDevice, hs.in));
+      CUDA_TRY(cudaEventRecord(ev_in, hs.in));
+      CUDA_TRY(cudaStreamWaitEvent(hs.comp, ev_in, 0));
+      const int s2 = run_plan(plan, direction, dxk, x_type, ld_x, dyk, y_type,
+                              ld_y, m, hs.comp);
       if (s2 != FM_OK) return s2;
-      CUDA_TRY(cudaEventRecord(ev_done, plan->hstream));
-      CUDA_TRY(cudaStreamWaitEvent(plan->hout, ev_done, 0));
+      CUDA_TRY(cudaEventRecord(ev_done, hs.comp));
+      CUDA_TRY(cudaStreamWaitEvent(hs.out, ev_done, 0));
       CUDA_TRY(cudaMemcpyAsync((char *)y + c0 * cy, dyk, m * cy,
-                               cudaMemcpyDeviceToHost, plan->hout));
+                               cudaMemcpyDeviceToHost, hs.out));
     }
-    CUDA_TRY(cudaStreamSynchronize(plan->hout));
-    CUDA_TRY(cudaStreamSynchronize(plan->hstream));
-    CUDA_TRY(cudaStreamSynchronize(plan->hin));
-    return fm_plan_check(plan);
+    CUDA_TRY(cudaStreamSynchronize(hs.out));
+    CUDA_TRY(cudaStreamSynchronize(hs.comp));
+    CUDA_TRY(cudaStreamSynchronize(hs.in));
+    return check_status(plan);
   });
-  if (st != FM_OK) drain();
+  // streams that may still hold copies into the caller's buffers are
+  // drained before any return
+  if (st != FM_OK)
+    for (cudaStream_t q : {hs.in, hs.comp, hs.out})
+      if (q) cudaStreamSynchronize(q);
+  if (switched && prev >= 0) cudaSetDevice(prev);
   return st;
 }
 
@@ -2402,6 +2514,7 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
     if (direction != FM_FORWARD && direction != FM_BACKWARD)
       fail(FM_ERR_VALUE, "invalid direction");
     if (num_cols <= 0) fail(FM_ERR_VALUE, "num_cols must be positive");
+    check_device(plan->device, "the plan");
     const cudaStream_t s = (cudaStream_t)stream;
     const i64 n_in = direction == FM_FORWARD ? plan->cols : plan->rows;
     const i64 n_out = direction == FM_FORWARD ? plan->rows : plan->cols;
@@ -2420,8 +2533,8 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
         const i64 cap = std::max<i64>(
             1, (512ll << 20) / (std::max(rs, rd) * plan->esz));
         const i64 M = std::min<i64>(num_cols, cap);
-        CUDA_TRY(cudaMalloc(&tsrc, (size_t)(rs * M * plan->esz)));
-        CUDA_TRY(cudaMalloc(&tdst, (size_t)(rd * M * plan->esz)));
+        CUDA_TRY(dev_malloc(&tsrc, (size_t)(rs * M * plan->esz)));
+        CUDA_TRY(dev_malloc(&tdst, (size_t)(rd * M * plan->esz)));
         // normal numbers (0x3F bytes) so that no fast path for zeros runs
         CUDA_TRY(cudaMemsetAsync(tsrc, 0x3F, (size_t)(rs * M * plan->esz), s));
         CUDA_TRY(cudaMemsetAsync(tdst, 0x3F, (size_t)(rd * M * plan->esz), s));
@@ -2482,17 +2595,38 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
 int fm_plan_check(fm_plan *plan) {
   return guarded([&]() {
     if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
-    if (!plan->err) return FM_OK;
-    int e = 0;
-    CUDA_TRY(cudaMemcpy(&e, plan->err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e != 0) {
-      CUDA_TRY(cudaMemset(plan->err, 0, sizeof(int)));
-      fail(FM_ERR_TIMEOUT,
-           "a bounded wait for a tile copy gave up; results of the affected "
-           "call are incomplete");
-    }
+    return check_status(plan);
+  });
+}
+
+int fm_plan_set_wait_limit(fm_plan *plan, int64_t polls) {
+  return guarded([&]() {
+    if (!plan) fail(FM_ERR_VALUE, "plan is NULL");
+    if (polls < 0) fail(FM_ERR_VALUE, "negative wait limit");
+    plan->wait_limit = polls;
     return FM_OK;
   });
+}
+
+int fm_release_host_staging(void) {
+  return guarded([&]() {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    HostStage &hs = host_stage(dev);
+    std::lock_guard<std::mutex> lock(hs.mu);
+    for (cudaStream_t q : {hs.in, hs.comp, hs.out})
+      if (q) CUDA_TRY(cudaStreamSynchronize(q));
+    if (hs.dx) cudaFree(hs.dx);
+    if (hs.dy) cudaFree(hs.dy);
+    hs.dx = hs.dy = nullptr;
+    hs.dx_cap = hs.dy_cap = 0;
+    return FM_OK;
+  });
+}
+
+int fm_debug_fail_allocation(int32_t after) {
+  g_alloc_skip.store(after < 0 ? -1 : (long long)after);
+  return FM_OK;
 }
 
 int fm_plan_destroy(fm_plan *plan) {
@@ -2595,6 +2729,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
       if (!P || P->ctype != ctype)
         fail(FM_ERR_VALUE, "fm_batch_create: plans must share one compute "
                            "type");
+      check_device(P->device, "a plan of the batch");
       size_t bytes = 0;
       if (num_cols[i] > 0)
         for (i64 r : P->scratch_rows)
@@ -2604,10 +2739,10 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
     }
     char *scratch = nullptr;
     if (op_off[num_ops]) {
-      CUDA_TRY(cudaMalloc(&scratch, op_off[num_ops]));
+      CUDA_TRY(dev_malloc(&scratch, op_off[num_ops]));
       B->allocs.push_back(scratch);
     }
-    CUDA_TRY(cudaMalloc(&B->status, 2 * sizeof(int)));
+    CUDA_TRY(dev_malloc(&B->status, 2 * sizeof(int)));
     B->allocs.push_back(B->status);
     CUDA_TRY(cudaMemset(B->status, 0, 2 * sizeof(int)));
     for (int i = 0; i < num_ops; ++i) {
@@ -2716,11 +2851,11 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
     fmk::Step *dsteps = nullptr;
     i64 *dstart = nullptr;
     int *dlevel = nullptr;
-    CUDA_TRY(cudaMalloc(&dsteps, steps.size() * sizeof(fmk::Step)));
+    CUDA_TRY(dev_malloc(&dsteps, steps.size() * sizeof(fmk::Step)));
     B->allocs.push_back(dsteps);
-    CUDA_TRY(cudaMalloc(&dstart, start.size() * sizeof(i64)));
+    CUDA_TRY(dev_malloc(&dstart, start.size() * sizeof(i64)));
     B->allocs.push_back(dstart);
-    CUDA_TRY(cudaMalloc(&dlevel, level.size() * sizeof(int)));
+    CUDA_TRY(dev_malloc(&dlevel, level.size() * sizeof(int)));
     B->allocs.push_back(dlevel);
     CUDA_TRY(cudaMemcpy(dsteps, steps.data(),
                         steps.size() * sizeof(fmk::Step),
@@ -2752,6 +2887,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
 int fm_batch_execute(fm_batch *batch, void *stream) {
   return guarded([&]() {
     if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    check_device(batch->device, "the batch");
     const cudaStream_t s = (cudaStream_t)stream;
     CUDA_TRY(cudaMemsetAsync(batch->status, 0, sizeof(int), s));
     CUDA_TRY(fmk::launch_batch(batch->launch, s));
@@ -2762,6 +2898,7 @@ int fm_batch_execute(fm_batch *batch, void *stream) {
 int fm_batch_execute_graph(fm_batch *batch, void *stream) {
   return guarded([&]() {
     if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    check_device(batch->device, "the batch");
     if (!batch->exec) {
       if (!batch->gstream)
         CUDA_TRY(cudaStreamCreateWithFlags(&batch->gstream,
@@ -2782,6 +2919,18 @@ int fm_batch_execute_graph(fm_batch *batch, void *stream) {
       CUDA_TRY(e4);
     }
     CUDA_TRY(cudaGraphLaunch(batch->exec, (cudaStream_t)stream));
+    return FM_OK;
+  });
+}
+
+int fm_batch_set_wait_limit(fm_batch *batch, int64_t polls) {
+  return guarded([&]() {
+    if (!batch) fail(FM_ERR_VALUE, "batch is NULL");
+    if (polls < 0) fail(FM_ERR_VALUE, "negative wait limit");
+    if (batch->exec)
+      fail(FM_ERR_VALUE, "the batch's graph is already captured with its "
+                         "wait limit");
+    batch->launch.wait_limit = polls;
     return FM_OK;
   });
 }
@@ -2819,6 +2968,6 @@ int fm_batch_destroy(fm_batch *batch) {
 
 const char *fm_last_error(void) { return g_err.c_str(); }
 
-int32_t fm_version(void) { return 101; }
+int32_t fm_version(void) { return 102; }
 
 }  // extern "C"

@@ -86,6 +86,7 @@ struct Step {
   int in_len, out_len;
   i64 V;         // vectors per column
   i64 num_cols;
+  long long wait_limit;  // polls of a bounded copy wait before it gives up
   int nops;
   int pad_;
   Op ops[FM_MAX_OPS];
@@ -1552,6 +1553,7 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 }
 
 // polls of a bounded mbarrier wait before a launch reports FM_ERR_TIMEOUT
+// (the default of Step::wait_limit; fm_plan_set_wait_limit changes it)
 #define FM_WAIT_LIMIT (1LL << 22)
 
 // ------------------------------------------------------------ the kernel
@@ -1671,7 +1673,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
         bool ok = true;
         if (tid < 32)
           ok = mbar_wait(smem_addr(bars + cur), (phase_bits >> cur) & 1u,
-                         FM_WAIT_LIMIT);
+                         p.wait_limit);
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
@@ -1748,7 +1750,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
   if (failed) {
     if (tid == 0 && p.err) atomicExch(p.err, FM_ERR_TIMEOUT);
     // let the loads still in flight (this tile and up to nbuf - 2 ahead)
-    // land before the CTA exits, again with bounded waits
+    // land before the CTA exits, again with bounded waits (of the default
+    // length, whatever limit made the first wait give up)
     for (int d = 0; d < NB - 1; ++d) {
       int k = cur + d;
       if (k >= NB) k -= NB;
@@ -1776,20 +1779,20 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
 // until all gridDim.x CTAs of this phase have arrived.  Returns false (and
 // records FM_ERR_TIMEOUT) if the wait gives up; the caller then returns.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target,
-                                             int *err) {
+                                             int *err, long long limit) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     atomicAdd(bar, 1u);
     unsigned v = 0;
-    int it = 0;
+    long long it = 0;
     for (;;) {
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];"
                    : "=r"(v)
                    : "l"(bar)
                    : "memory");
-      if (v >= target || ++it > FM_WAIT_LIMIT) break;
+      if (v >= target || ++it > limit) break;
       __nanosleep(64);
     }
     ok = v >= target;
@@ -1849,7 +1852,7 @@ template <class E, int CLS>
 __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
     batch_kernel(const Step *__restrict__ steps, const i64 *__restrict__ start,
                  const int *__restrict__ level, int nlev, unsigned *bar,
-                 int *err, int max_B, size_t max_tile) {
+                 int *err, int max_B, size_t max_tile, long long wait_limit) {
   extern __shared__ __align__(128) unsigned char fm_smem[];
   const int tid = threadIdx.x, T = blockDim.x;
   Step *const sst = reinterpret_cast<Step *>(fm_smem);
@@ -1926,7 +1929,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       kc = kn;
     }
     if (l + 1 < nlev &&
-        !grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err))
+        !grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err, wait_limit))
       return;
   }
 }

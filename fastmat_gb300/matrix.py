@@ -93,6 +93,58 @@ def _numpy_dtype(tdt):
     raise TypeError("unsupported tensor dtype %s" % tdt)
 
 
+#: outputs at least this large come from page-locked host memory
+_PINNED_MIN_BYTES = 1 << 20
+
+
+def _host_output(rows, cols, dt):
+    """Fortran-ordered (rows x cols) result array.  Large ones live in
+    page-locked memory from torch's caching host allocator (reused across
+    calls once freed), so the device-to-host copies of fm_execute_host run
+    asynchronously, overlapped with the transform of the next column
+    chunk; the array keeps its torch storage alive."""
+    dt = np.dtype(dt)
+    if rows * cols * dt.itemsize >= _PINNED_MIN_BYTES:
+        torch = _torch()
+        t = torch.empty((cols, rows), dtype=_torch_dtype(dt),
+                        pin_memory=True)
+        return t.numpy().T
+    return np.empty((rows, cols), dtype=dt, order='F')
+
+
+def _device_index(device=None):
+    """Index of a CUDA device (torch.device, int or None = current); -1
+    when no CUDA device is visible."""
+    torch = _torch()
+    if device is None:
+        return torch.cuda.current_device() if torch.cuda.is_available() else -1
+    if isinstance(device, int):
+        return device
+    d = torch.device(device)
+    if d.type != 'cuda':
+        raise ValueError("not a CUDA device: %s" % (device,))
+    return d.index if d.index is not None else torch.cuda.current_device()
+
+
+class _device_scope:
+    """Make device `dev` current inside the block (no-op for dev < 0)."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.ctx = None
+
+    def __enter__(self):
+        if self.dev >= 0:
+            self.ctx = _torch().cuda.device(self.dev)
+            self.ctx.__enter__()
+        return self
+
+    def __exit__(self, *exc):
+        if self.ctx is not None:
+            return self.ctx.__exit__(*exc)
+        return False
+
+
 def _compute_code(out_dtype, precision='native'):
     """Element type a plan computes in for a given output type.
 
@@ -269,15 +321,20 @@ class Matrix:
             out = T.single(out)
         return out
 
-    def plan(self, out_dtype=np.complex128):
-        """The native plan computing in the type of ``out_dtype``."""
+    def plan(self, out_dtype=np.complex128, device=None):
+        """The native plan computing in the type of ``out_dtype`` on a CUDA
+        device (default: the current one).  A plan's constants live on the
+        device it was built on, so plans are kept per device; the plan is
+        built with that device current."""
         code = _compute_code(out_dtype, self._precision)
-        p = self._plans.get(code)
+        dev = _device_index(device)
+        p = self._plans.get((dev, code))
         if p is None:
             b = _Builder()
             root = self._emit(b)
-            p = _native.Plan(b.nodes, b.children, root, code, b.keep)
-            self._plans[code] = p
+            with _device_scope(dev):
+                p = _native.Plan(b.nodes, b.children, root, code, b.keep)
+            self._plans[(dev, code)] = p
         return p
 
     def autotune(self, num_cols=1, out_dtype=None, cache=True):
@@ -291,8 +348,21 @@ class Matrix:
         return tuning.autotune(self.plan(out_dtype), num_cols, cache)
 
     def forward(self, arrX):
-        """y = A x.  1-D or 2-D numpy arrays or CUDA torch tensors."""
+        """y = A x.  1-D or 2-D numpy arrays or CUDA torch tensors.
+
+        numpy inputs are transformed synchronously and a failure the kernels
+        record on the device (a bounded wait that gave up) raises here.  CUDA
+        tensors are transformed asynchronously on the current stream, like
+        any torch operation; ``check()`` synchronises and raises such a
+        failure."""
         return self._transform(arrX, _native.FORWARD)
+
+    def check(self):
+        """Synchronise with the device and raise RuntimeError if a kernel of
+        one of this operator's plans recorded a failure since the last
+        check (results of the affected calls are incomplete)."""
+        for p in list(self._plans.values()):
+            p.check()
 
     def backward(self, arrX):
         """y = A^H x."""
@@ -321,20 +391,15 @@ class Matrix:
         if M == 0:
             y = np.empty((n_out, 0), dtype=out_dt, order='F')
             return y
+        # (an operator without a GPU form raises NotImplementedError here)
         plan = self.plan(out_dt)
-        torch = _torch()
-        if not torch.cuda.is_available():
+        if not _torch().cuda.is_available():
             raise RuntimeError("fastmat_gb300 needs a CUDA device")
         xf = np.asfortranarray(x2)
-        xt = torch.from_numpy(xf.T).to('cuda')
-        yt = torch.empty((M, n_out), dtype=_torch_dtype(out_dt),
-                         device='cuda')
-        stream = torch.cuda.current_stream().cuda_stream
-        plan.execute(direction, xt.data_ptr(), _native.DTYPE_CODE[xf.dtype],
-                     n_req, yt.data_ptr(), _native.DTYPE_CODE[out_dt], n_out,
-                     M, stream)
-        y = yt.cpu().numpy().T
-        plan.check()
+        y = _host_output(n_out, M, out_dt)
+        # fm_execute_host: column chunks pipelined over copy-in, compute and
+        # copy-out streams, synchronous, device status checked
+        plan.execute_host(direction, xf, y)
         return y.reshape(n_out) if flat else y
 
     def _transform_device(self, x, direction):
@@ -365,7 +430,8 @@ class Matrix:
         yt = torch.empty((M, n_out), dtype=_torch_dtype(out_dt),
                          device=x.device)
         if M > 0:
-            plan = self.plan(out_dt)
+            # the plan of the tensor's device, launched with it current
+            plan = self.plan(out_dt, device=x.device)
             with torch.cuda.device(x.device):
                 stream = torch.cuda.current_stream().cuda_stream
                 plan.execute(direction, xc.data_ptr(),

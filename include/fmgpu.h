@@ -135,9 +135,18 @@ typedef struct fm_plan fm_plan;
 
 /* Compile an operator tree.  `compute_type` is the element type the plan
  * computes and stores intermediates in (FM_F32, FM_F64, FM_C64, FM_C128 or
- * FM_I64 for integer-only trees).  Node vectors are host pointers, copied
- * during the call; the caller may free them afterwards.  Device constants
- * (spectra, chirps, twiddles, index maps) are built on the current device. */
+ * FM_I64 for integer-only trees, or one of the forms below).  A tree that
+ * only moves data (Permutation, Partial, Eye, Hermitian, Conjugate, scalars
+ * +-1 / +-i, and Product / Sum / Kron / Blocks of such trees) computes in
+ * its I/O type even when FM_F64_DF, FM_C128_DF or FM_F32_TC is asked for:
+ * its outputs are then input elements bit for bit (or IEEE sums of them, in
+ * fastmat's order), as fastmat's gathers produce them
+ * (fastmat/Permutation.pyx:120-124, fastmat/Partial.pyx:268-294).  Node
+ * vectors are host pointers, copied during the call; the caller may free
+ * them afterwards.  Device constants (spectra, chirps, twiddles, index
+ * maps) are built on the current device, the plan's device: every call
+ * that launches work for the plan must be made with that device current
+ * (FM_ERR_VALUE otherwise), except fm_execute_host, which switches to it. */
 int fm_plan_create(const fm_node *nodes, int32_t num_nodes,
                    const int32_t *children, int32_t num_children,
                    int32_t root, int32_t compute_type, fm_plan **out_plan);
@@ -196,14 +205,24 @@ int fm_execute_static(fm_plan *plan, int32_t direction,
                       int64_t num_cols, void *stream);
 
 /* Same as fm_execute with HOST buffers: copies x to the device, runs the
- * plan and copies the result back into y before returning (synchronous).
- * Large calls are split into column chunks pipelined over three streams
- * (copy in, compute, copy out), so with page-locked host buffers the
- * copies of one chunk overlap the transform of the next. */
+ * plan and copies the result back into y before returning (synchronous),
+ * and reports a device-side failure of the call (as fm_plan_check).  Runs on
+ * the plan's device, whatever device is current, and leaves the current
+ * device as it was.  Large calls are split into column chunks pipelined over
+ * three streams (copy in, compute, copy out), so with page-locked host
+ * buffers the copies of one chunk overlap the transform of the next.  The
+ * device operand buffers and streams are kept per device, shared by all
+ * plans and sized by the largest call so far, until the process exits;
+ * calls on one device take turns. */
 int fm_execute_host(fm_plan *plan, int32_t direction,
                     const void *x, int32_t x_type, int64_t ld_x,
                     void *y, int32_t y_type, int64_t ld_y,
                     int64_t num_cols);
+
+/* Free the device operand buffers fm_execute_host keeps for the current
+ * device (for example after a one-off large call); the next host call
+ * allocates them again.  The reference has no counterpart. */
+int fm_release_host_staging(void);
 
 /* Tile shape of launch `launch` of a direction: vectors per tile and the
  * depth (2..4) of its copy ring, keeping the launch's tile layout;
@@ -238,6 +257,16 @@ int fm_plan_autotune(fm_plan *plan, int32_t direction, int64_t num_cols,
  * every call; callers of the asynchronous entry points check after they
  * synchronise.  The reference has no device and no counterpart. */
 int fm_plan_check(fm_plan *plan);
+
+/* Number of polls a bounded wait of this plan's kernels (a tile copy's
+ * mbarrier) makes before it gives up and the launch records FM_ERR_TIMEOUT
+ * for fm_plan_check; default 2^22 (each poll may suspend the thread for up to
+ * about a microsecond).  A kernel that gives up still waits, with the
+ * default limit, for the copies it has in flight, then returns.  0 makes the
+ * first wait give up at once: the failure path can be exercised without a
+ * fault.  Takes effect from the next launch.  The reference has no device
+ * and no counterpart. */
+int fm_plan_set_wait_limit(fm_plan *plan, int64_t polls);
 
 int fm_plan_destroy(fm_plan *plan);
 
@@ -283,6 +312,10 @@ int fm_batch_execute(fm_batch *batch, void *stream);
 int fm_batch_execute_graph(fm_batch *batch, void *stream);
 /* Synchronises; FM_ERR_TIMEOUT if a bounded wait of the batch gave up. */
 int fm_batch_check(fm_batch *batch);
+/* Polls of the batch's grid-barrier waits before a CTA gives up, records
+ * FM_ERR_TIMEOUT and returns (default 2^22; 0: at once).  Must be set
+ * before the first fm_batch_execute_graph, which captures the launch. */
+int fm_batch_set_wait_limit(fm_batch *batch, int64_t polls);
 /* Launches of the bound plans it replaces, levels, tiles. */
 int fm_batch_get_info(const fm_batch *batch, int64_t *num_launches,
                       int64_t *num_levels, int64_t *num_tiles);
@@ -312,6 +345,13 @@ int fm_reduce_mulconj(int64_t A, int64_t n, int64_t Cc, int64_t num_cols,
                       int32_t type, const void *u, int64_t ld_u,
                       const void *v, int64_t ld_v, void *out, double scale,
                       const void *d, void *w, int64_t ld_w, void *stream);
+
+/* Test hook for the out-of-memory path: after `after` more device
+ * allocations of this library succeed, the next one fails as if the device
+ * were full (the call then returns FM_ERR_NOMEM and frees what it had
+ * allocated); after < 0 disarms it.  One-shot, process-wide.  The reference
+ * has no counterpart. */
+int fm_debug_fail_allocation(int32_t after);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *fm_last_error(void);

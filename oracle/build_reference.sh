@@ -9,8 +9,15 @@
 # Nothing produced here is committed (baseline/_ref/ is git-ignored) and
 # nothing here runs on the GPU machine; the golden fixtures under
 # tests/golden/ are what travels.
+#
+# Usage: oracle/build_reference.sh <path of the fastmat source tree>
+#        (or FASTMAT_REFERENCE=<path> oracle/build_reference.sh)
 set -euo pipefail
-REF=${FASTMAT_REFERENCE:-/root/reference}
+REF=${1:-${FASTMAT_REFERENCE:-}}
+if [ -z "$REF" ] || [ ! -d "$REF/fastmat" ]; then
+  echo "usage: $0 <fastmat source tree> (or set FASTMAT_REFERENCE)" >&2
+  exit 2
+fi
 HERE=$(cd "$(dirname "$0")/.." && pwd)
 DST="$HERE/baseline/_ref/src"
 if [ -f "$DST/.built" ]; then echo "reference already built in $DST"; exit 0; fi

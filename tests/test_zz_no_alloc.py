@@ -7,7 +7,11 @@ multi-launch plans need in a fixed 16 MiB array compiled into the library.
 
 This file is collected last so that, if it fails, a run stopping at the
 first failure has already run every other test.  It calls both entry points
-through the C ABI (ctypes) on device buffers and compares them."""
+through the C ABI (ctypes) on device buffers and compares them.  Each case
+runs the static entry point on a FRESH plan before that plan has ever run
+through fm_execute (so the plan owns no scratch buffer the static path could
+borrow) and checks that the device's free memory does not change across the
+two static calls."""
 
 import ctypes
 
@@ -21,52 +25,80 @@ pytestmark = pytest.mark.gpu
 STATIC_BYTES = 16 << 20
 
 
-def _plan_with_scratch(n=20000):
-    """A long circulant: its four-step convolution keeps an L-row scratch
-    buffer per column between launches (L = 65536 here)."""
+def _cplx(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+def _operator(kind):
+    """Operators whose plans keep scratch between launches: a long circulant
+    (four-step convolution, an L-row buffer per column, L = 65536) and a Sum
+    of two of them (also the accumulating copy that reads its destination
+    first)."""
     import fastmat_gb300 as fg
     rng = np.random.default_rng(11)
-    c = rng.standard_normal(n) + 1j * rng.standard_normal(n)
-    op = fg.Circulant(c)
-    plan = op.plan(np.complex128)
-    assert plan.info().scratch_bytes_per_col > 0
-    return op, plan
+    n = 20000
+    c1, c2 = _cplx(rng, n), _cplx(rng, n)
+    if kind == 'circulant':
+        return fg.Circulant(c1), fo.Circulant(c1)
+    return (fg.Sum(fg.Circulant(c1), fg.Circulant(c2)),
+            fo.Sum(fo.Circulant(c1), fo.Circulant(c2)))
 
 
-def _run(lib_fn, plan, xt, yt, m, stream):
+def _run(lib_fn, plan, direction, xt, yt, m, stream):
     from fastmat_gb300 import _native
     n_in, n_out = xt.shape[1], yt.shape[1]
-    return lib_fn(plan.handle, _native.FORWARD, ctypes.c_void_p(xt.data_ptr()),
+    return lib_fn(plan.handle, direction, ctypes.c_void_p(xt.data_ptr()),
                   _native.FM_C128, n_in, ctypes.c_void_p(yt.data_ptr()),
                   _native.FM_C128, n_out, m, ctypes.c_void_p(stream))
 
 
-def test_static_entry_matches_fm_execute_on_two_calls_in_a_row():
+@pytest.mark.parametrize('direction', [0, 1], ids=['forward', 'backward'])
+@pytest.mark.parametrize('kind', ['circulant', 'sum'])
+def test_static_entry_matches_fm_execute_on_two_calls_in_a_row(kind,
+                                                               direction):
     import torch
     from fastmat_gb300 import _native
     lib = _native.load()
-    op, plan = _plan_with_scratch()
-    n = op.numRows
     m = 4
-    per_col = plan.info().scratch_bytes_per_col
-    assert per_col * m <= STATIC_BYTES
     stream = torch.cuda.current_stream().cuda_stream
-    rng = np.random.default_rng(5)
+    rng = np.random.default_rng(5 + direction)
+    op, oop = _operator(kind)
+    n = op.numRows
+    xs = [torch.from_numpy(_cplx(rng, m, n)).cuda() for _ in range(2)]
+    y_sta = [torch.full_like(x, float('nan')) for x in xs]
+    y_ref = [torch.empty_like(x) for x in xs]
+    # warm-up on another plan of the same operator: loads the kernels and the
+    # static array's module, so only the calls under test remain
+    warm = op.plan(np.complex128)
+    assert _run(lib.fm_execute_static, warm, direction, xs[0], y_ref[0], m,
+                stream) == 0
+    # a fresh plan: it has never run, so it owns no scratch buffer
+    op.__dict__.pop('_plans', None)
+    op._plans = {}
+    plan = op.plan(np.complex128)
+    assert plan is not warm
+    per_col = plan.info().scratch_bytes_per_col
+    assert per_col > 0 and per_col * m <= STATIC_BYTES
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     for call in range(2):
-        x = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
-        xt = torch.from_numpy(x).cuda()  # row k = column k (column-major)
-        y_ref = torch.empty_like(xt)
-        y_sta = torch.full_like(xt, float('nan'))
-        assert _run(lib.fm_execute, plan, xt, y_ref, m, stream) == 0
-        st = _run(lib.fm_execute_static, plan, xt, y_sta, m, stream)
+        st = _run(lib.fm_execute_static, plan, direction, xs[call],
+                  y_sta[call], m, stream)
         assert st == 0, lib.fm_last_error()
-        torch.cuda.synchronize()
-        a, b = y_ref.cpu().numpy(), y_sta.cpu().numpy()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0, \
+        "fm_execute_static allocated device memory"
+    # the allocating entry point on the same plan, afterwards
+    for call in range(2):
+        assert _run(lib.fm_execute, plan, direction, xs[call], y_ref[call], m,
+                    stream) == 0
+    plan.check()
+    for call in range(2):
+        a, b = y_ref[call].cpu().numpy(), y_sta[call].cpu().numpy()
         assert np.all(np.isfinite(b))
         assert fo.rel_err(b, a) <= 1e-12, (call, fo.rel_err(b, a))
-        # and both against the FFT definition of the circulant product
-        want = np.fft.ifft(np.fft.fft(op.tenC)[None, :] *
-                           np.fft.fft(x, axis=1), axis=1)
+        x = xs[call].cpu().numpy().T
+        want = (oop.forward(x) if direction == 0 else oop.backward(x)).T
         assert fo.rel_err(b, want) <= 1e-12
 
 
@@ -74,13 +106,14 @@ def test_static_entry_rejects_oversize_calls():
     import torch
     from fastmat_gb300 import _native
     lib = _native.load()
-    op, plan = _plan_with_scratch()
+    op, _ = _operator('circulant')
+    plan = op.plan(np.complex128)
     per_col = plan.info().scratch_bytes_per_col
     m = STATIC_BYTES // per_col + 1
     n = op.numRows
     xt = torch.zeros((m, n), dtype=torch.complex128, device='cuda')
     yt = torch.zeros_like(xt)
-    st = _run(lib.fm_execute_static, plan, xt, yt, m,
+    st = _run(lib.fm_execute_static, plan, 0, xt, yt, m,
               torch.cuda.current_stream().cuda_stream)
     assert st == _native.FM_ERR_VALUE
     assert b'static' in lib.fm_last_error()
