@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "fm_rconv.cuh"
 #include "fm_vprog.cuh"
 
 namespace fmk {
@@ -54,6 +55,13 @@ struct SpStep {
 };
 cudaError_t launch_spmv(int ctype, const SpStep &p, int group,
                         cudaStream_t s);
+
+// register-resident convolution (fm_rconv.cuh): lengths it is built for
+// (powers of two from rconv_min_len to rconv_max_len; 0: not for this type)
+// and one launch
+int rconv_max_len(int ctype);
+int rconv_min_len(int ctype);
+cudaError_t launch_rconv(int ctype, const RcStep &p, cudaStream_t s);
 
 // largest FFT radix the kernels of a compute type are built with (see
 // MinBlocks / Radix16 in fm_vprog.cuh): 8 for single precision and

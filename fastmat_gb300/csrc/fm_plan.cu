@@ -232,8 +232,14 @@ struct LStep {
   int src, dst;  // 0 = x, 1 = y, >= 2 scratch
   // first row of the launch's operand inside its buffer (Blocks segments)
   i64 src_off = 0, dst_off = 0;
-  // 0: vector program (vprog_kernel); 1: CSR sparse product (spmv_kernel)
+  // 0: vector program (vprog_kernel); 1: CSR sparse product (spmv_kernel);
+  // 2: register-resident convolution (rconv_kernel), whose `st` still holds
+  // the equivalent vector program (run by batches)
   int kind = 0;
+  int rc_L = 0;
+  const void *rc_spec = nullptr, *rc_tw = nullptr;  // spectrum in rconv order
+  const void *rc_pre = nullptr, *rc_post = nullptr;
+  int rc_conj_in = 0, rc_conj_out = 0, rc_spec_conj = 0;
   const i64 *sp_ptr = nullptr, *sp_idx = nullptr;
   const void *sp_val = nullptr;
   i64 sp_rows = 0;
@@ -1489,8 +1495,80 @@ class Planner {
     return (cls == 0 || cls == 2) ? lmax_ / 2 : lmax_;
   }
 
+  // A program that is one circular convolution of contiguous vectors,
+  // [conj] [pre] [zero pad] FFT(-1), spectrum product, FFT(+1) [post]
+  // [conj], with a length the register kernel is built for, runs there
+  // (kind 2); its spectrum is stored in that kernel's digit order.
+  void try_rconv(LStep &ls, const std::vector<fmk::Op> &ops) {
+    const int ct = P_->ctype;
+    const int lmax = fmk::rconv_max_len(ct), lmin = fmk::rconv_min_len(ct);
+    const fmk::Step &st = ls.st;
+    if (!lmax || st.vin.Cc != 1 || st.vout.Cc != 1 || st.map_in ||
+        st.map_out || st.out_mode != 0)
+      return;
+    auto whole = [](const fmk::Op &o) {
+      return o.kind == fmk::OP_MUL && o.div == 1 && o.mod == 1 &&
+             o.stride == 0;
+    };
+    auto is = [&](size_t i, int kind) {
+      return i < ops.size() && ops[i].kind == kind;
+    };
+    size_t i = 0;
+    bool cj_in = false, cj_out = false;
+    const void *pre = nullptr, *post = nullptr;
+    if (is(i, fmk::OP_CONJ)) cj_in = true, ++i;
+    if (i < ops.size() && whole(ops[i]) && ops[i].sign == 0 &&
+        (is(i + 1, fmk::OP_ZPAD) || is(i + 1, fmk::OP_FFT)))
+      pre = ops[i++].ptr;
+    if (is(i, fmk::OP_ZPAD)) {
+      if (ops[i].len != st.in_len) return;
+      ++i;
+    }
+    if (!is(i, fmk::OP_FFT) || ops[i].sign != -1) return;
+    const int L = ops[i].len;
+    ++i;
+    if (i >= ops.size() || !whole(ops[i]) || ops[i].len != L) return;
+    const fmk::Op &sm = ops[i++];
+    if (!is(i, fmk::OP_FFT) || ops[i].sign != 1 || ops[i].len != L) return;
+    ++i;
+    if (i < ops.size() && whole(ops[i]) && ops[i].sign == 0)
+      post = ops[i++].ptr;
+    if (is(i, fmk::OP_CONJ)) cj_out = true, ++i;
+    if (i != ops.size()) return;
+    if (!is_pow2(L) || L < lmin || L > lmax || st.L != L ||
+        st.in_len > L || st.out_len > L)
+      return;
+    // products in the program index points of a vector, the launch's by
+    // rows: the same when a column holds one vector
+    if ((pre && (st.pre || st.vin.A != 1)) ||
+        (post && (st.post || st.vout.A != 1)) || (cj_in && st.conj_in) ||
+        (cj_out && st.conj_out))
+      return;
+    const int P = fmk::rconv_min_len(ct);
+    std::vector<int> rad;
+    for (int rest = L; rest > 1;) {
+      const int r = std::min(rest, P);
+      rad.push_back(r);
+      rest /= r;
+    }
+    const Perm &pm = perm_for(rad);
+    const std::vector<cd> &S = host_vec_.at(sm.ptr);
+    std::vector<cd> w((size_t)L);
+    for (int q = 0; q < L; ++q) w[(size_t)q] = S[(size_t)pm.nat[q]];
+    ls.rc_spec = upload(w);
+    ls.rc_tw = twiddle(L);
+    ls.rc_L = L;
+    ls.rc_pre = pre;
+    ls.rc_post = post;
+    ls.rc_conj_in = cj_in;
+    ls.rc_conj_out = cj_out;
+    ls.rc_spec_conj = sm.sign;
+    ls.kind = 2;
+  }
+
   void finish(LStep &ls, const std::vector<fmk::Op> &ops_in) {
     fmk::Step &st = ls.st;
+    try_rconv(ls, ops_in);
     std::vector<fmk::Op> ops = ops_in;
     st.out_pos = finalize(ops);
     if ((int)ops.size() > FM_MAX_OPS)
@@ -1905,6 +1983,41 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 
 // Finish a bound launch (TMA descriptors, status word) and issue it.
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
+  if (ls.kind == 2) {
+    fmk::RcStep rc;
+    memset(&rc, 0, sizeof(rc));
+    rc.src = st.src;
+    rc.dst = st.dst;
+    rc.ld_src = st.ld_src;
+    rc.ld_dst = st.ld_dst;
+    rc.src_type = st.src_type;
+    rc.dst_type = st.dst_type;
+    rc.A = st.vin.A;
+    rc.in_stride = st.vin.n;
+    rc.out_stride = st.vout.n;
+    rc.in_rows = st.in_rows;
+    rc.out_rows = st.out_rows;
+    rc.in_len = st.in_len;
+    rc.out_len = st.out_len;
+    rc.num_cols = st.num_cols;
+    rc.spec = ls.rc_spec;
+    rc.tw = ls.rc_tw;
+    rc.pre = st.pre ? st.pre : ls.rc_pre;
+    rc.post = st.post ? st.post : ls.rc_post;
+    rc.err = P->err;
+    rc.spec_conj = ls.rc_spec_conj;
+    rc.conj_in = st.conj_in || ls.rc_conj_in;
+    rc.conj_out = st.conj_out || ls.rc_conj_out;
+    rc.has_scale = st.has_scale;
+    rc.accumulate = st.accumulate;
+    rc.L = ls.rc_L;
+    rc.scale_re = st.scale_re;
+    rc.scale_im = st.scale_im;
+    if (rc.A * rc.num_cols >= 0x7fffffffLL)
+      fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
+    CUDA_TRY(fmk::launch_rconv(P->ctype, rc, s));
+    return;
+  }
   if (ls.kind == 1) {
     fmk::SpStep sp;
     sp.ptr = ls.sp_ptr;
@@ -2670,6 +2783,21 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
         s += line;
         continue;
       }
+      if (ls.kind == 2) {
+        snprintf(line, sizeof(line),
+                 "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,"
+                 "%lld) rconv L=%d acc=%d:",
+                 ls.src, ls.dst, st.vin.A, st.vin.n, st.vin.Cc, st.vout.A,
+                 st.vout.n, st.vout.Cc, ls.rc_L, st.accumulate);
+        s += line;
+        s += ls.rc_conj_in || st.conj_in ? " conj" : "";
+        s += ls.rc_pre || st.pre ? " pre" : "";
+        s += " fft-conv";
+        s += ls.rc_post || st.post ? " post" : "";
+        s += ls.rc_conj_out || st.conj_out ? " conj" : "";
+        s += "\n";
+        continue;
+      }
       snprintf(line, sizeof(line),
                "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,%lld) "
                "L=%d B=%d threads=%d smem=%zu cls=%d acc=%d:",
@@ -2769,10 +2897,10 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
       }
       int level = 0;
       for (const LStep &ls0 : P->steps[dir]) {
-        if (ls0.kind != 0)
+        if (ls0.kind == 1)
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: sparse operators run "
                                    "outside batches");
-        LStep ls = ls0;
+        LStep ls = ls0;  // register convolutions run as their vector program
         if (!configure(esz, ls, 0, 0, false, 0, false))
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "
                                    "vector-major tile shape");

@@ -1,0 +1,339 @@
+// Register-resident circular convolution of contiguous power-of-two vectors:
+//
+//     y = post . conj_out(scale * IFFT(S . FFT(zpad(pre . conj_in(x)))))
+//
+// the program a Circulant / Toeplitz / Bluestein apply lowers to when its
+// length fits one warp (fastmat applies it as fft, product, ifft:
+// fastmat/Circulant.pyx:127-133, fastmat/Toeplitz.pyx:255-268).  The generic
+// vector-program kernel runs every FFT stage as a pass through a shared-
+// memory tile with run-time index arithmetic; here the whole transform pair
+// lives in registers:
+//
+//   * a vector of L points is held by G = L / P lanes of one warp, P points
+//     per lane (16 complex64 or 8 double-float complex), loaded straight
+//     from global memory in natural order (lane g holds points g + G r), so
+//     a warp covers 32 / G vectors;
+//   * the forward FFT is an in-place decimation-in-frequency over the radix
+//     sequence (P, P, ..., rest): every stage is P / R radix-R butterflies
+//     per lane in registers, with the twiddles of its butterflies (which
+//     depend only on the lane) from a table in shared memory; between stages
+//     the lanes of a vector exchange points through a per-warp shared-memory
+//     buffer (warp barriers only);
+//   * after the last forward stage each lane holds its points in digit-
+//     reversed order; they are multiplied by the spectrum stored in that
+//     order, and the inverse transform (decimation in time, the stages in
+//     reverse) starts on the same registers: the last forward and the first
+//     inverse stage share their butterflies, so no exchange between them;
+//   * the inverse leaves lane g with points g + G r again, stored straight
+//     to global memory.
+//
+// Positions follow the in-place DIF of the vector-program kernel
+// (fm_vprog.cuh): stage i with radix R, Mprev = L / (R_0 ... R_{i-1}) and
+// M = Mprev / R takes, for block K and t < M, the points K Mprev + t + M r.
+// Lane g's butterflies at stage i are w = g + G u (u < P / R); because M
+// divides G, t = g mod M and the position is a per-lane base plus a
+// compile-time offset u G R + M r.
+#pragma once
+
+#include "fm_vprog.cuh"
+
+namespace fmk {
+
+// One launch of the register convolution (built by the planner from a
+// vector-program step whose program is [zero pad] FFT, product, inverse FFT
+// on contiguous vectors).
+struct RcStep {
+  const void *src;
+  void *dst;
+  i64 ld_src, ld_dst;
+  int src_type, dst_type;
+  i64 A;                      // vectors per column
+  i64 in_stride, out_stride;  // rows from one vector of a column to the next
+  i64 in_rows, out_rows;      // rows of a column that exist / are written
+  int in_len, out_len;        // points of a vector read (rest: zero) / stored
+  i64 num_cols;
+  const void *spec;  // spectrum / L in the forward stages' output order
+  const void *tw;    // tw[j] = exp(-2 pi i j / L), j < L
+  const void *pre, *post;  // loader / storer products indexed by row
+  int *err;
+  int spec_conj, conj_in, conj_out, has_scale, accumulate;
+  int L;
+  double scale_re, scale_im;
+};
+
+// ---- compile-time plan: P points per lane, radices (P, P, ..., rest)
+template <class E> struct RcLane {
+  static constexpr int P = sizeof(E) == 8 ? 16 : 8;
+};
+__host__ __device__ constexpr int rc_stages(int L, int P) {
+  return L <= P ? 1 : 1 + rc_stages(L / P, P);
+}
+__host__ __device__ constexpr int rc_radix(int i, int L, int P) {
+  return i == 0 ? (L < P ? L : P) : rc_radix(i - 1, L / P, P);
+}
+// L / (R_0 ... R_{i-1})
+__host__ __device__ constexpr int rc_mprev(int i, int L, int P) {
+  return i == 0 ? L : rc_mprev(i - 1, L, P) / rc_radix(i - 1, L, P);
+}
+__host__ __device__ constexpr int rc_log2(int n) {
+  return n <= 1 ? 0 : 1 + rc_log2(n / 2);
+}
+
+// shared-memory position of point p of a vector buffer: one spare point per
+// 128 bytes spreads strided butterfly accesses over the banks
+template <class E> __device__ __forceinline__ int rc_pad(int p) {
+  constexpr int SH = sizeof(E) == 8 ? 4 : 3;
+  return p + (p >> SH);
+}
+template <class E, int L> struct RcBuf {
+  static constexpr int SH = sizeof(E) == 8 ? 4 : 3;
+  // padded length; the extra half-granule row shift makes consecutive
+  // vectors of a warp start on different banks
+  static constexpr int Lp = L + (L >> SH) + (L >= (1 << SH) ? 0 : 1);
+};
+
+// Stage `I` of the forward (INV = false: DFT, then twiddles of the outputs)
+// or inverse (INV = true: conjugate twiddles of the inputs, then DFT with
+// sign +1) transform on the lane's P registers, in place: register
+// u R + r holds position base + u G R + M r before and after.
+template <class E, int L, int I, bool INV>
+__device__ __forceinline__ void rc_stage(E (&x)[RcLane<E>::P], int g,
+                                         const E *__restrict__ stw) {
+  constexpr int P = RcLane<E>::P;
+  constexpr int R = rc_radix(I, L, P);
+  constexpr int Mprev = rc_mprev(I, L, P);
+  constexpr int M = Mprev / R;
+  constexpr int NB = P / R;
+  constexpr int TS = L / Mprev;  // table stride of w_Mprev
+  constexpr int SG = INV ? +1 : -1;
+  typedef typename Lazy<E>::type LC;
+  const int t = g & (M - 1);
+  // the twiddles w_Mprev^(t k), k < R, are the same for all u
+  E w[R];
+  if constexpr (M > 1) {
+#pragma unroll
+    for (int k = 1; k < R; ++k) w[k] = stw[t * k * TS];
+  }
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    LC v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = to_lazy(x[u * R + r]);
+    if constexpr (INV && M > 1) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul_lazy<+1>(v[k], w[k]);
+    }
+    dif_stages<R, R / 2>(v, SG);  // v[i] = output brev(i)
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      LC y = v[i];
+      const int k = brev<R>(i);
+      if constexpr (!INV && M > 1) {
+        if (k != 0) y = cmul_lazy<-1>(y, w[k]);
+      }
+      x[u * R + k] = from_lazy(y);
+    }
+  }
+}
+
+// position base of lane g at stage I (see the file comment)
+template <class E, int L, int I>
+__device__ __forceinline__ int rc_base(int g) {
+  constexpr int P = RcLane<E>::P;
+  constexpr int Mprev = rc_mprev(I, L, P);
+  constexpr int M = Mprev / rc_radix(I, L, P);
+  return (g >> rc_log2(M)) * Mprev + (g & (M - 1));
+}
+template <class E, int L, int I>
+__device__ __forceinline__ int rc_off(int j) {  // register j = u R + r
+  constexpr int P = RcLane<E>::P;
+  constexpr int R = rc_radix(I, L, P);
+  constexpr int G = L / P;
+  constexpr int M = rc_mprev(I, L, P) / R;
+  return (j / R) * G * R + M * (j % R);
+}
+
+// Registers laid out for stage IA -> shared buffer -> registers laid out
+// for stage IB (warp barriers: the lanes of a vector are in one warp).
+template <class E, int L, int IA, int IB>
+__device__ __forceinline__ void rc_exchange(E (&x)[RcLane<E>::P], E *buf,
+                                            int g) {
+  constexpr int P = RcLane<E>::P;
+  const int ba = rc_base<E, L, IA>(g), bb = rc_base<E, L, IB>(g);
+#pragma unroll
+  for (int j = 0; j < P; ++j) buf[rc_pad<E>(ba + rc_off<E, L, IA>(j))] = x[j];
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < P; ++j) x[j] = buf[rc_pad<E>(bb + rc_off<E, L, IB>(j))];
+  __syncwarp();
+}
+
+template <class E, int L, int I>
+__device__ __forceinline__ void rc_forward(E (&x)[RcLane<E>::P], E *buf, int g,
+                                           const E *stw) {
+  rc_stage<E, L, I, false>(x, g, stw);
+  constexpr int S = rc_stages(L, RcLane<E>::P);
+  if constexpr (I + 1 < S) {
+    rc_exchange<E, L, I, I + 1>(x, buf, g);
+    rc_forward<E, L, I + 1>(x, buf, g, stw);
+  }
+}
+template <class E, int L, int I>
+__device__ __forceinline__ void rc_inverse(E (&x)[RcLane<E>::P], E *buf, int g,
+                                           const E *stw) {
+  rc_stage<E, L, I, true>(x, g, stw);
+  if constexpr (I > 0) {
+    rc_exchange<E, L, I, I - 1>(x, buf, g);
+    rc_inverse<E, L, I - 1>(x, buf, g, stw);
+  }
+}
+
+// threads per CTA and CTAs per SM of the register convolution
+#define FM_RC_THREADS 256
+template <class E> struct RcOcc {
+  static constexpr int v = sizeof(E) == 8 ? 3 : 2;
+};
+
+template <class E, int L>
+__host__ __device__ constexpr size_t rc_smem() {
+  return (size_t)(2 * L + (FM_RC_THREADS / 32) * (32 / (L / RcLane<E>::P)) *
+                              RcBuf<E, L>::Lp) *
+         sizeof(E);
+}
+
+template <class E, int L>
+__global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E>::v))
+    rconv_kernel(const __grid_constant__ RcStep p) {
+  constexpr int P = RcLane<E>::P;
+  constexpr int G = L / P;
+  static_assert(G >= 1 && G <= 32 && (G & (G - 1)) == 0, "lanes per vector");
+  constexpr int VPW = 32 / G;
+  constexpr int S = rc_stages(L, P);
+  constexpr int Lp = RcBuf<E, L>::Lp;
+  extern __shared__ __align__(128) unsigned char fm_smem[];
+  E *stw = reinterpret_cast<E *>(fm_smem);
+  E *sspec = stw + L;
+  E *sx = sspec + L;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    stw[i] = ((const E *)p.tw)[i];
+    sspec[i] = ((const E *)p.spec)[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int q = lane / G, g = lane % G;
+  E *buf = sx + (wib * VPW + q) * Lp;
+  const i64 NV = p.A * p.num_cols;
+  const FDiv dA((unsigned)p.A);
+  const i64 nwarps = (i64)gridDim.x * (blockDim.x >> 5);
+  const bool raw_in = p.src_type == Tr<E>::code;
+  const bool raw_out = p.dst_type == Tr<E>::code && !p.accumulate;
+  const E cs = scalar_of<E>(p.scale_re, p.scale_im);
+  for (i64 vb = ((i64)blockIdx.x * (blockDim.x >> 5) + wib) * VPW; vb < NV;
+       vb += nwarps * VPW) {
+    const i64 v = vb + q;
+    const bool act = v < NV;
+    unsigned m = 0, a = 0;
+    if (act) {
+      m = dA.div((unsigned)v);
+      a = (unsigned)v - m * (unsigned)p.A;
+    }
+    const i64 rin0 = (i64)a * p.in_stride;   // row of point 0 in the column
+    const i64 rout0 = (i64)a * p.out_stride;
+    E x[P];
+    int sexp = 0;
+    // ---- load points g + G r (zero beyond the vector / the column)
+    if constexpr (Emu<E>::v) {
+      // float64 / complex128 bits, scaled per vector by the power of two of
+      // its largest exponent (the double-float exponent range is float's)
+      double2 d[P];
+      int emax = 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const int j = g + G * r;
+        const i64 row = rin0 + j;
+        const bool ok = act && j < p.in_len && row < p.in_rows;
+        d[r] = make_double2(0., 0.);
+        if (ok) {
+          if (raw_in) {
+            d[r] = ((const double2 *)p.src)[(i64)m * p.ld_src + row];
+          } else {
+            double re, im;
+            split(load_as<double2>(p.src, p.src_type,
+                                   (i64)m * p.ld_src + row),
+                  re, im);
+            d[r] = make_double2(re, im);
+          }
+        }
+        const int e1 = dexp(d[r].x), e2 = dexp(d[r].y);
+        emax = max(emax, max(e1, e2));
+      }
+#pragma unroll
+      for (int o = G / 2; o >= 1; o /= 2)
+        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o, G));
+      sexp = emax > 0 ? emax - 1023 : 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        E val = dfc{d2df_scaled(d[r].x, sexp), d2df_scaled(d[r].y, sexp)};
+        const i64 row = rin0 + g + G * r;
+        if (p.conj_in) val = conjv(val);
+        if (p.pre && row < p.in_rows)
+          val = mulv(val, ((const E *)p.pre)[row], false);
+        x[r] = val;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const int j = g + G * r;
+        const i64 row = rin0 + j;
+        E val = zero<E>();
+        if (act && j < p.in_len && row < p.in_rows) {
+          const i64 idx = (i64)m * p.ld_src + row;
+          val = raw_in ? ((const E *)p.src)[idx]
+                       : load_as<E>(p.src, p.src_type, idx);
+          if (p.conj_in) val = conjv(val);
+          if (p.pre) val = mulv(val, ((const E *)p.pre)[row], false);
+        }
+        x[r] = val;
+      }
+    }
+    // ---- forward transform, spectrum product, inverse transform
+    rc_forward<E, L, 0>(x, buf, g, stw);
+    {
+      const int bs = rc_base<E, L, S - 1>(g);
+#pragma unroll
+      for (int j = 0; j < P; ++j)
+        x[j] = mulv(x[j], sspec[bs + rc_off<E, L, S - 1>(j)],
+                    p.spec_conj != 0);
+    }
+    rc_inverse<E, L, S - 1>(x, buf, g, stw);
+    // ---- store points g + G r
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const int j = g + G * r;
+        const i64 row = rout0 + j;
+        if (j >= p.out_len || row >= p.out_rows) continue;
+        E val = x[r];
+        if (p.post) val = mulv(val, ((const E *)p.post)[row], false);
+        if (p.has_scale) val = mulv(val, cs, false);
+        if (p.conj_out) val = conjv(val);
+        const i64 idx = (i64)m * p.ld_dst + row;
+        if constexpr (Emu<E>::v) {
+          if (raw_out)
+            ((double2 *)p.dst)[idx] = make_double2(
+                df2d_scaled(val.x, sexp), df2d_scaled(val.y, sexp));
+          else
+            store_as<E>(p.dst, p.dst_type, idx, val, p.accumulate != 0,
+                        sexp);
+        } else {
+          if (raw_out)
+            ((E *)p.dst)[idx] = val;
+          else
+            store_as<E>(p.dst, p.dst_type, idx, val, p.accumulate != 0);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace fmk

@@ -34,9 +34,8 @@ def _data(rng, n, m, dt):
     # in every column: far more than the 2^126 span of one float32 exponent
     big = 300 if dt in (np.float64, np.complex128) else 37
     x *= 10.0 ** rng.integers(-big, big, size=(n, m))
-    x[0] = 1.0
-    x[1] = 10.0 ** -big
-    x[2] = -(10.0 ** big)
+    for i, v in enumerate((1.0, 10.0 ** -big, -(10.0 ** big))[:n]):
+        x[i] = v
     return x.astype(dt)
 
 

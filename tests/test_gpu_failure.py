@@ -41,7 +41,8 @@ def test_wait_limit_zero_reports_timeout_then_recovers(expr):
         dt = np.complex128
         x = cplx(rng, 1024, 64)
     elif expr == 'kron_strided':   # strided mode: TMA boxes + mbarrier
-        op = fg.Kron(fg.Fourier(64), fg.Eye(256))
+        # complex64 throughout: the loads need no type conversion
+        op = fg.Kron(fg.Fourier(64), fg.Eye(256), precision='fp32')
         oop = fo.Kron(fo.Fourier(64), fo.Eye(256))
         dt = np.complex64
         x = cplx(rng, op.numCols, 8).astype(np.complex64)
