@@ -35,6 +35,8 @@
 // compile-time offset u G R + M r.
 #pragma once
 
+#include <type_traits>
+
 #include "fm_vprog.cuh"
 
 namespace fmk {
@@ -190,19 +192,21 @@ __device__ __forceinline__ void rc_inverse(E (&x)[RcLane<E>::P], E *buf, int g,
 
 // threads per CTA and CTAs per SM of the register convolution
 #define FM_RC_THREADS 256
-template <class E> struct RcOcc {
-  static constexpr int v = sizeof(E) == 8 ? 3 : 2;
+template <class E, int L> struct RcOcc {
+  static constexpr int v = sizeof(E) == 8 && L < 512 ? 3 : 2;
 };
 
+// shared memory: twiddle and spectrum tables, then per warp an input slot
+// (the next vectors, copied in ahead) and an exchange buffer
 template <class E, int L>
 __host__ __device__ constexpr size_t rc_smem() {
-  return (size_t)(2 * L + (FM_RC_THREADS / 32) * (32 / (L / RcLane<E>::P)) *
-                              RcBuf<E, L>::Lp) *
+  return (size_t)(2 * L + 2 * (FM_RC_THREADS / 32) *
+                              (32 / (L / RcLane<E>::P)) * RcBuf<E, L>::Lp) *
          sizeof(E);
 }
 
 template <class E, int L>
-__global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E>::v))
+__global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
     rconv_kernel(const __grid_constant__ RcStep p) {
   constexpr int P = RcLane<E>::P;
   constexpr int G = L / P;
@@ -221,15 +225,43 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E>::v))
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int q = lane / G, g = lane % G;
-  E *buf = sx + (wib * VPW + q) * Lp;
+  E *buf = sx + (wib * VPW + q) * Lp;  // exchange buffer of this vector
+  // input slot of this vector: the raw bits of its points, natural order
+  E *slot = sx + ((FM_RC_THREADS / 32) + wib) * VPW * Lp + q * Lp;
   const i64 NV = p.A * p.num_cols;
   const FDiv dA((unsigned)p.A);
   const i64 nwarps = (i64)gridDim.x * (blockDim.x >> 5);
+  // inputs already in the buffers' type are copied in one batch ahead by
+  // cp.async (zero-filled beyond the vector / the column); others are
+  // converted by synchronous loads
   const bool raw_in = p.src_type == Tr<E>::code;
   const bool raw_out = p.dst_type == Tr<E>::code && !p.accumulate;
   const E cs = scalar_of<E>(p.scale_re, p.scale_im);
-  for (i64 vb = ((i64)blockIdx.x * (blockDim.x >> 5) + wib) * VPW; vb < NV;
-       vb += nwarps * VPW) {
+  typedef typename std::conditional<Emu<E>::v, double2, E>::type Raw;
+  static_assert(sizeof(Raw) == sizeof(E), "raw element size");
+  auto prefetch = [&](i64 vn) {
+    const i64 v = vn + q;
+    unsigned m = 0, a = 0;
+    const bool act = v < NV;
+    if (act) {
+      m = dA.div((unsigned)v);
+      a = (unsigned)v - m * (unsigned)p.A;
+    }
+    const Raw *src = (const Raw *)p.src + (i64)m * p.ld_src +
+                     (i64)a * p.in_stride;
+    const i64 left = p.in_rows - (i64)a * p.in_stride;
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      const int j = g + G * r;
+      const bool ok = act && j < p.in_len && j < left;
+      cp_async<sizeof(E)>(slot + j, ok ? (const void *)(src + j)
+                                       : (const void *)p.src, ok);
+    }
+    cp_async_commit();
+  };
+  const i64 v0 = ((i64)blockIdx.x * (blockDim.x >> 5) + wib) * VPW;
+  if (raw_in && v0 < NV) prefetch(v0);
+  for (i64 vb = v0; vb < NV; vb += nwarps * VPW) {
     const i64 v = vb + q;
     const bool act = v < NV;
     unsigned m = 0, a = 0;
@@ -240,60 +272,64 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E>::v))
     const i64 rin0 = (i64)a * p.in_stride;   // row of point 0 in the column
     const i64 rout0 = (i64)a * p.out_stride;
     E x[P];
-    int sexp = 0;
-    // ---- load points g + G r (zero beyond the vector / the column)
-    if constexpr (Emu<E>::v) {
-      // float64 / complex128 bits, scaled per vector by the power of two of
-      // its largest exponent (the double-float exponent range is float's)
-      double2 d[P];
-      int emax = 0;
+    Raw d[P];
+    if (raw_in) {
+      cp_async_wait<0>();
+      __syncwarp();
 #pragma unroll
-      for (int r = 0; r < P; ++r) {
-        const int j = g + G * r;
-        const i64 row = rin0 + j;
-        const bool ok = act && j < p.in_len && row < p.in_rows;
-        d[r] = make_double2(0., 0.);
-        if (ok) {
-          if (raw_in) {
-            d[r] = ((const double2 *)p.src)[(i64)m * p.ld_src + row];
-          } else {
-            double re, im;
-            split(load_as<double2>(p.src, p.src_type,
-                                   (i64)m * p.ld_src + row),
-                  re, im);
-            d[r] = make_double2(re, im);
-          }
-        }
-        const int e1 = dexp(d[r].x), e2 = dexp(d[r].y);
-        emax = max(emax, max(e1, e2));
-      }
-#pragma unroll
-      for (int o = G / 2; o >= 1; o /= 2)
-        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o, G));
-      sexp = emax > 0 ? emax - 1023 : 0;
-#pragma unroll
-      for (int r = 0; r < P; ++r) {
-        E val = dfc{d2df_scaled(d[r].x, sexp), d2df_scaled(d[r].y, sexp)};
-        const i64 row = rin0 + g + G * r;
-        if (p.conj_in) val = conjv(val);
-        if (p.pre && row < p.in_rows)
-          val = mulv(val, ((const E *)p.pre)[row], false);
-        x[r] = val;
-      }
+      for (int r = 0; r < P; ++r)
+        d[r] = reinterpret_cast<const Raw *>(slot)[g + G * r];
+      __syncwarp();
+      if (vb + nwarps * VPW < NV) prefetch(vb + nwarps * VPW);
     } else {
 #pragma unroll
       for (int r = 0; r < P; ++r) {
         const int j = g + G * r;
         const i64 row = rin0 + j;
-        E val = zero<E>();
-        if (act && j < p.in_len && row < p.in_rows) {
-          const i64 idx = (i64)m * p.ld_src + row;
-          val = raw_in ? ((const E *)p.src)[idx]
-                       : load_as<E>(p.src, p.src_type, idx);
-          if (p.conj_in) val = conjv(val);
-          if (p.pre) val = mulv(val, ((const E *)p.pre)[row], false);
+        Raw val;
+        if constexpr (Emu<E>::v) {
+          val = make_double2(0., 0.);
+          if (act && j < p.in_len && row < p.in_rows) {
+            double re, im;
+            split(load_as<double2>(p.src, p.src_type,
+                                   (i64)m * p.ld_src + row),
+                  re, im);
+            val = make_double2(re, im);
+          }
+        } else {
+          val = zero<E>();
+          if (act && j < p.in_len && row < p.in_rows)
+            val = load_as<E>(p.src, p.src_type, (i64)m * p.ld_src + row);
         }
-        x[r] = val;
+        d[r] = val;
+      }
+    }
+    int sexp = 0;
+    if constexpr (Emu<E>::v) {
+      // float64 / complex128 bits, scaled per vector by the power of two of
+      // its largest exponent (the double-float exponent range is float's)
+      int emax = 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r)
+        emax = max(emax, max(dexp(d[r].x), dexp(d[r].y)));
+#pragma unroll
+      for (int o = G / 2; o >= 1; o /= 2)
+        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o, G));
+      sexp = emax > 0 ? emax - 1023 : 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r)
+        x[r] = dfc{d2df_scaled(d[r].x, sexp), d2df_scaled(d[r].y, sexp)};
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; ++r) x[r] = d[r];
+    }
+    if (p.conj_in || p.pre) {
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const i64 row = rin0 + g + G * r;
+        if (p.conj_in) x[r] = conjv(x[r]);
+        if (p.pre && g + G * r < p.in_len && row < p.in_rows)
+          x[r] = mulv(x[r], ((const E *)p.pre)[row], false);
       }
     }
     // ---- forward transform, spectrum product, inverse transform
