@@ -295,104 +295,346 @@ def _dist_setup(torch, world, local, backend=None):
     return (lambda: None), (lambda v: v)
 
 
+_LAUNCH_RE = None
+
+
+def launch_bytes(plan, n_in, n_out, M, esz_x, esz_y):
+    """Algorithmic bytes of every launch of a forward call: the rows of its
+    input view read once and the rows of its output view written once, at
+    the element size of the buffer each lives in (x, y or scratch in the
+    plan's I/O type), times the columns."""
+    import re
+    global _LAUNCH_RE
+    if _LAUNCH_RE is None:
+        _LAUNCH_RE = re.compile(
+            r'launch src=(\d+) dst=(\d+)(?: in=\((\d+),(\d+),(\d+)\) '
+            r'out=\((\d+),(\d+),(\d+)\))?')
+    esz_io = {16: 8, 17: 16, 18: 4}.get(plan.compute_type)
+    if esz_io is None:
+        esz_io = np.dtype(fg_dtype(plan.compute_type)).itemsize
+    out = []
+    for ln in plan.describe(0).splitlines():
+        m = _LAUNCH_RE.match(ln)
+        if not m:
+            continue
+        src, dst = int(m.group(1)), int(m.group(2))
+        if m.group(3) is not None:
+            rin = int(m.group(3)) * int(m.group(4)) * int(m.group(5))
+            rout = int(m.group(6)) * int(m.group(7)) * int(m.group(8))
+        else:  # sparse product: its operands' shapes
+            rin, rout = n_in, n_out
+        rin = min(rin, n_in) if src == 0 else rin
+        rout = min(rout, n_out) if dst == 1 else rout
+        b_in = rin * (esz_x if src == 0 else esz_y if src == 1 else esz_io)
+        b_out = rout * (esz_y if dst == 1 else esz_io)
+        out.append(M * (b_in + b_out))
+    return out
+
+
+def fg_dtype(code):
+    import fastmat_gb300 as fg
+    return fg._native.CODE_DTYPE[code]
+
+
+def _per_launch(fg, torch, op, xt, yt, dt, out_dt, reps=5):
+    plan = op.plan(out_dt)
+    code = fg._native.DTYPE_CODE
+    runs = [plan.execute_profiled(
+        fg._native.FORWARD, xt.data_ptr(), code[np.dtype(dt)], op.numCols,
+        yt.data_ptr(), code[out_dt], op.numRows, xt.shape[1],
+        torch.cuda.current_stream().cuda_stream) for _ in range(reps)]
+    plan.check()
+    return plan, np.mean(np.array(runs), axis=0)
+
+
+def roofline_of(fg, plan, per_launch, n_in, n_out, M, dt, out_dt, peak,
+                peak_kind, workload, form, what='vprog'):
+    """Roofline of the dominant launch: its algorithmic bytes over its
+    CUDA-event time, against the measured copy bandwidth."""
+    lb = launch_bytes(plan, n_in, n_out, M, np.dtype(dt).itemsize,
+                      np.dtype(out_dt).itemsize)
+    if len(lb) != len(per_launch):
+        lb = [(n_in * np.dtype(dt).itemsize +
+               n_out * np.dtype(out_dt).itemsize) * M] * len(per_launch)
+    k = int(np.argmax(per_launch))
+    ach = lb[k] / (per_launch[k] * 1e-3) / 1e9
+    kernel = 'rconv' if 'rconv' in plan.describe(0).splitlines()[k] \
+        else what
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_kind": peak_kind,
+            "traffic": ncu_traffic(workload, form, k + 1),
+            "kernel": "%s launch %d of %d" % (kernel, k + 1,
+                                              len(per_launch)),
+            "kernel_ms": float(per_launch[k]),
+            "kernel_bytes": int(lb[k]),
+            "launch_ms": [round(float(v), 4) for v in per_launch]}
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a.astype(np.complex128) - b)) /
+                 np.max(np.abs(b)))
+
+
+def measure_form(torch, fg, name, prec, dt, M, args, barrier, allmax, peak,
+                 peak_kind, seed, form, clocks=None, x=None):
+    """One form of one workload: CUDA-event step time on device-resident
+    data, per-launch times, roofline of the dominant launch."""
+    build_fn = WORKLOADS[name][0]
+    op, _, _ = build_fn(fg, prec)
+    out_dt = np.dtype(op._output_dtype(np.dtype(dt)))
+    if not args.no_autotune:
+        op.autotune(M, out_dtype=out_dt)
+    if x is None:
+        x = make_input(op.numCols, M, dt, seed)
+    xt = torch.from_numpy(np.ascontiguousarray(x.T)).cuda().t()
+    if clocks is not None:
+        clocks.start()
+    ms, yt = time_device(torch, op, xt, args.steps, args.warmup, barrier)
+    clk = clocks.stop() if clocks is not None else None
+    ms = allmax(ms)
+    nbytes = (op.numCols * np.dtype(dt).itemsize +
+              op.numRows * out_dt.itemsize) * M
+    plan, per_launch = _per_launch(fg, torch, op, xt, yt, dt, out_dt)
+    return dict(op=op, x=x, xt=xt, y=yt, ms=ms, bytes=nbytes, clk=clk,
+                plan=plan, per_launch=per_launch, out_dt=out_dt,
+                n_launch=len(per_launch),
+                roofline=roofline_of(fg, plan, per_launch, op.numCols,
+                                     op.numRows, M, dt, out_dt, peak,
+                                     peak_kind, name, form))
+
+
+def _oracle_columns(name, x, cols):
+    """The oracle's forward on selected columns of x (float64 / complex128
+    unless the input is single precision)."""
+    op, _ = _oracle_workload(name)
+    return op.forward(np.asfortranarray(x[:, cols]))
+
+
+def summarize(r, world):
+    return {"ms_per_step": r['ms'],
+            "value": world * r['bytes'] / (r['ms'] * 1e-3) / 1e9,
+            "unit": "GB/s", "roofline": r['roofline']}
+
+
+def config_circulant(torch, fg, args, ctx):
+    """cfg: Circulant(1024) on 16 columns, FP64 drop-in and FP32 form."""
+    M = 16
+    r64 = measure_form(torch, fg, 'circulant', 'native', np.complex128, M,
+                       args, *ctx, seed=0, form='fp64')
+    r32 = measure_form(torch, fg, 'circulant', 'fp32', np.complex64, M,
+                       args, *ctx, seed=0, form='fp32')
+    ref = _oracle_columns('circulant', r64['x'], list(range(M)))
+    out = summarize(r64, 1)
+    out.update({
+        "workload": WORKLOADS['circulant'][3], "dtype": "c128 I/O, "
+        "double-float arithmetic (~2^-48)",
+        "note": "launch-bound (0.5 MiB of operands per step)",
+        "rel_err_vs_oracle": rel_err(r64['y'].cpu().numpy(), ref),
+        "oracle_sample": "all %d columns" % M,
+        "fp32_form": dict(summarize(r32, 1),
+                          rel_err_vs_oracle=rel_err(r32['y'].cpu().numpy(),
+                                                    ref))})
+    out["gpu_launches_per_step"] = r64['n_launch']
+    return out
+
+
+def config_hadamard(torch, fg, args, ctx):
+    """cfg: Hadamard(22) on 64 float32 columns: FP64 (double-float), FP32
+    (butterflies in fastmat's order: bit-exact to its float32 result) and
+    BF16 tensor-core forms."""
+    from oracle import fm_oracle as fo
+    M = 64
+    x32 = make_input(1 << 22, M, np.float32, 3)
+    r32 = measure_form(torch, fg, 'hadamard', 'fp32', np.float32, M, args,
+                       *ctx, seed=3, form='fp32', x=x32)
+    rbf = measure_form(torch, fg, 'hadamard', 'bf16', np.float32, M, args,
+                       *ctx, seed=3, form='bf16', x=x32)
+    y32 = r32.pop('y').cpu().numpy()
+    ybf = rbf.pop('y').cpu().numpy()
+    for r in (r32, rbf):
+        del r['xt']
+    torch.cuda.empty_cache()
+    r64 = measure_form(torch, fg, 'hadamard', 'native', np.float64, M, args,
+                       *ctx, seed=3, form='fp64', x=x32.astype(np.float64))
+    y64 = r64['y'].cpu().numpy()
+    cols = [0, M - 1]
+    H = fo.Hadamard(22)
+    ref = H.forward(x32[:, cols].astype(np.float64))
+    ref32 = H.forward(np.asfortranarray(x32[:, cols]))
+    out = summarize(r64, 1)
+    out.update({
+        "workload": WORKLOADS['hadamard'][3],
+        "dtype": "f64 I/O, double-float arithmetic (~2^-48)",
+        "rel_err_vs_oracle": rel_err(y64[:, cols], ref),
+        "oracle_sample": "columns %s" % cols,
+        "fp32_form": dict(summarize(r32, 1), dtype="f32",
+                          speedup_vs_fp64=r64['ms'] / r32['ms'],
+                          rel_err_vs_oracle=rel_err(y32[:, cols], ref),
+                          bit_exact_vs_float32_oracle=bool(
+                              np.array_equal(y32[:, cols], ref32))),
+        "bf16_form": dict(summarize(rbf, 1),
+                          dtype="f32 data, bf16 x3 MMA, f32 accumulation",
+                          rel_err_vs_oracle=rel_err(ybf[:, cols], ref))})
+    del r64, y64
+    torch.cuda.empty_cache()
+    return out
+
+
+def config_chain(torch, fg, args, ctx):
+    """cfg: Partial(rows) Circulant Diag, N = 2^18, 32 columns: fused
+    forward (FP64 and FP32) and the differentiable form (complex64)."""
+    M = 32
+    r64 = measure_form(torch, fg, 'chain', 'native', np.complex128, M,
+                       args, *ctx, seed=4, form='fp64')
+    r32 = measure_form(torch, fg, 'chain', 'fp32', np.complex64, M, args,
+                       *ctx, seed=4, form='fp32')
+    cols = [0, 1]
+    ref = _oracle_columns('chain', r64['x'], cols)
+    out = summarize(r64, 1)
+    out.update({
+        "workload": WORKLOADS['chain'][3],
+        "dtype": "c128 I/O, double-float arithmetic (~2^-48)",
+        "rel_err_vs_oracle": rel_err(r64['y'].cpu().numpy()[:, cols], ref),
+        "oracle_sample": "columns %s" % cols,
+        "fp32_form": dict(summarize(r32, 1),
+                          rel_err_vs_oracle=rel_err(
+                              r32['y'].cpu().numpy()[:, cols], ref)),
+        "differentiable": measure_grad(torch, fg, args)})
+    return out
+
+
+def config_batched(torch, fg, args, ctx):
+    """cfg: 512 operators in one persistent launch (complex64, CUDA graph)
+    against the FP64 path applied operator by operator."""
+    from oracle import fm_oracle as fo
+    _, _, peak, peak_kind = ctx
+    specs = batched_specs(seed=0)
+    ops32 = batched_ops(fg, specs, 'fp32')
+    rng = np.random.default_rng(100)
+    xs = []
+    for op, m in ops32:
+        x = (rng.standard_normal((m, op.numCols)) +
+             1j * rng.standard_normal((m, op.numCols))).astype(np.complex64)
+        xs.append(torch.from_numpy(x).cuda().t())
+    nbytes = sum((op.numCols + op.numRows) * m * 8 for op, m in ops32)
+    batch = fg.Batch([(op, x) for (op, _), x in zip(ops32, xs)])
+    launches, levels, tiles = batch.info()
+    ms = _time_events(torch, lambda: batch.run(graph=True), args.steps,
+                      args.warmup)
+    batch.check()
+    ys = batch.outputs
+    ops64 = batched_ops(fg, specs)
+
+    def per_op64():
+        for (op, _), x in zip(ops64, xs):
+            op.forward(x)
+
+    ms64 = _time_events(torch, per_op64, 2, 1)
+    # oracle on a sample: every 16th operator with all its columns
+    sample = list(range(0, len(specs), 16))
+    oops = batched_ops(fo, specs)
+    err = 0.0
+    for i in sample:
+        x = xs[i].cpu().numpy().astype(np.complex128)
+        err = max(err, rel_err(ys[i].cpu().numpy(), oops[i][0].forward(x)))
+    ach = nbytes / (ms * 1e-3) / 1e9
+    return {"workload": WORKLOADS['batched'][3], "dtype": "c64",
+            "ms_per_step": ms, "value": ach, "unit": "GB/s",
+            "operators": len(ops32), "plan_launches_replaced": launches,
+            "levels": levels, "tiles": tiles,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak,
+                         "peak_kind": peak_kind,
+                         "traffic": ncu_traffic('batched', 'fp32', 1),
+                         "kernel": "batch_kernel (one cooperative launch)"},
+            "rel_err_vs_oracle": err,
+            "oracle_sample": "%d of %d operators (every 16th), all their "
+                             "columns" % (len(sample), len(specs)),
+            "fp64_per_operator": {"ms_per_step": ms64,
+                                  "speedup_of_batch": ms64 / ms}}
+
+
+def e2e_class_api(torch, fg, op, dt, M, args, barrier, allmax, seed):
+    """The drop-in call a user makes, op.forward(ndarray), on a page-locked
+    host input: every step copies X to the device and Y back (the pipelined
+    host entry point fm_execute_host); the result array is page-locked
+    memory reused from torch's caching host allocator after warm-up."""
+    n_in = op.numCols
+    xh = torch.empty((M, n_in), dtype=fg.matrix._torch_dtype(dt)) \
+        .pin_memory()
+    xh.numpy()[:] = make_input(n_in, M, dt, seed).T
+    xa = xh.numpy().T
+    for _ in range(args.warmup):
+        y = op.forward(xa)
+    del y
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        y = op.forward(xa)
+    t1 = time.perf_counter()
+    barrier()
+    return allmax((t1 - t0) * 1e3 / args.steps), xa, y
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_info()
     barrier, allmax = _dist_setup(torch, world, local)
     import fastmat_gb300 as fg
-    build_fn, dt64, dt32, desc = WORKLOADS[args.workload]
-    op64, M, _ = build_fn(fg, 'native')
-    op32, _, _ = build_fn(fg, 'fp32')
-    n_in, n_out = op64.numCols, op64.numRows
-
+    name = args.workload
+    build_fn, dt64, dt32, desc = WORKLOADS[name]
+    _, M, _ = build_fn(fg, 'native')
     peak, peak_kind = measured_peak()
-    results = {}
+    ctx = (barrier, allmax, peak, peak_kind)
     dev = torch.cuda.current_device()
     uuid = getattr(torch.cuda.get_device_properties(dev), 'uuid', None)
     clocks = ClockSampler('GPU-%s' % uuid if uuid is not None else dev)
-    ref_y = None
-    for name, op, dt in (('fp64', op64, dt64), ('fp32', op32, dt32)):
-        # plan creation includes the autotuner's choice of tile shapes
-        if not args.no_autotune:
-            op.autotune(M, out_dtype=op._output_dtype(np.dtype(dt)))
-        x = make_input(n_in, M, dt, 1000 + rank)
-        xt = torch.from_numpy(x.T).cuda().t()  # column-major device tensor
-        if name == 'fp64':
-            clocks.start()
-        ms, yt = time_device(torch, op, xt, args.steps, args.warmup, barrier)
-        if name == 'fp64':
-            clk = clocks.stop()
-        ms = allmax(ms)
-        out_dt = np.dtype(op._output_dtype(np.dtype(dt)))
-        nbytes = (n_in * M * np.dtype(dt).itemsize +
-                  n_out * M * out_dt.itemsize)
-        # per-launch timing of the same call (CUDA events between launches)
-        plan = op.plan(out_dt)
-        code = fg._native.DTYPE_CODE
-        launches = []
-        for _ in range(max(1, min(args.steps, 5))):
-            launches.append(plan.execute_profiled(
-                fg._native.FORWARD, xt.data_ptr(), code[np.dtype(dt)], n_in,
-                yt.data_ptr(), code[out_dt], n_out, M,
-                torch.cuda.current_stream().cuda_stream))
-        per_launch = np.mean(np.array(launches), axis=0)
-        results[name] = dict(ms=ms, bytes=nbytes, launches=per_launch,
-                             n_launch=len(per_launch), out_dt=out_dt, dt=dt,
-                             plan=plan, y=yt)
-        if name == 'fp64':
-            ref_y = yt
-    # relative error of the FP32 form against FP64: fresh calls on the same
-    # seeded input (rounded to single precision for the FP32 form)
-    xe = make_input(n_in, M, dt64, 1000 + rank)
-    y64 = op64.forward(torch.from_numpy(xe.T).cuda().t()).cpu().numpy()
-    y32 = op32.forward(torch.from_numpy(
-        xe.astype(dt32).T).cuda().t()).cpu().numpy()
-    rel = float(np.max(np.abs(y32.astype(y64.dtype) - y64)) /
-                np.max(np.abs(y64)))
-    del y32
+    seed = 1000 + rank
+    r64 = measure_form(torch, fg, name, 'native', dt64, M, args, *ctx,
+                       seed=seed, form='fp64', clocks=clocks)
+    r32 = measure_form(torch, fg, name, 'fp32', dt32, M, args, *ctx,
+                       seed=seed, form='fp32')
+    # accuracy: both forms against the oracle on column 0 (the FP32 form's
+    # input is the same data rounded to single precision)
+    y64 = r64['y'][:, 0].cpu().numpy()
+    y32 = r32['y'][:, 0].cpu().numpy()
+    ref = _oracle_columns(name, r64['x'], [0])[:, 0]
+    rel64, rel32 = rel_err(y64, ref), rel_err(y32, ref)
+    rel32_64 = rel_err(y32, y64)
+    for r in (r64, r32):
+        del r['xt'], r['y']
+    torch.cuda.empty_cache()
 
-    # e2e: host C ABI with pinned host buffers, copies inside the timed region
-    e2e = None
-    r64 = results['fp64']
-    xh = torch.empty((M, n_in), dtype=fg.matrix._torch_dtype(dt64)) \
-        .pin_memory()
-    xh.numpy()[:] = make_input(n_in, M, dt64, 1000 + rank).T
-    yh = torch.empty((M, n_out), dtype=fg.matrix._torch_dtype(
-        r64['out_dt'])).pin_memory()
-    xa = xh.numpy().T
-    ya = yh.numpy().T
-    plan64 = r64['plan']
+    # e2e through the class API and through the C ABI, pinned host buffers
+    op64 = r64['op']
+    e2e_ms, xa, ya = e2e_class_api(torch, fg, op64, dt64, M, args, barrier,
+                                   allmax, seed)
+    yc = torch.empty((M, op64.numRows),
+                     dtype=fg.matrix._torch_dtype(r64['out_dt'])) \
+        .pin_memory().numpy().T
     for _ in range(args.warmup):
-        plan64.execute_host(fg._native.FORWARD, xa, ya)
-    barrier()
+        r64['plan'].execute_host(fg._native.FORWARD, xa, yc)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        plan64.execute_host(fg._native.FORWARD, xa, ya)
-    t1 = time.perf_counter()
-    barrier()
-    e2e_ms = allmax((t1 - t0) * 1e3 / args.steps)
+        r64['plan'].execute_host(fg._native.FORWARD, xa, yc)
+    cabi_ms = allmax((time.perf_counter() - t0) * 1e3 / args.steps)
+    assert np.array_equal(ya, yc)
+    del xa, ya, yc
     e2e = {"value": world * r64['bytes'] / (e2e_ms * 1e-3) / 1e9,
            "unit": "GB/s", "ms_per_step": e2e_ms,
-           "h2d_bytes_per_step": int(n_in * M * np.dtype(dt64).itemsize),
-           "d2h_bytes_per_step": int(n_out * M * r64['out_dt'].itemsize),
-           "path": "fm_execute_host (C ABI), pinned host buffers"}
+           "h2d_bytes_per_step": int(op64.numCols * M *
+                                     np.dtype(dt64).itemsize),
+           "d2h_bytes_per_step": int(op64.numRows * M *
+                                     r64['out_dt'].itemsize),
+           "path": "class API %s.forward(ndarray) on a page-locked input "
+                   "(fm_execute_host pipeline: column chunks over copy-in, "
+                   "compute and copy-out streams)" % type(op64).__name__,
+           "c_abi_fm_execute_host": {
+               "ms_per_step": cabi_ms,
+               "value": world * r64['bytes'] / (cabi_ms * 1e-3) / 1e9}}
 
-    def roofline(r, form):
-        shares = r['launches'] / r['launches'].sum()
-        k = int(np.argmax(r['launches']))
-        kern_ms = float(r['launches'][k])
-        # every launch of this workload reads X-sized data and writes
-        # Y-sized data once; its algorithmic bytes are the step's bytes
-        achieved = r['bytes'] / (kern_ms * 1e-3) / 1e9
-        return {"bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(args.workload, form, k + 1),
-                "peak_kind": peak_kind,
-                "kernel": "vprog launch %d of %d" % (k + 1, len(shares)),
-                "kernel_ms": kern_ms,
-                "launch_ms": [round(float(v), 4) for v in r['launches']]}
-
-    r32 = results['fp32']
     line = {
         "metric": "matvec GB/s vs HBM roofline; FP32 vs FP64 GPU speedup at "
                   "rel err <=1e-5",
@@ -401,71 +643,50 @@ def run_gpu(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": r64['ms'],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128" if np.dtype(dt64).kind == 'c' else "f64",
+        "dtype": ("c128" if np.dtype(dt64).kind == 'c' else "f64") +
+                 " (I/O; double-float arithmetic on the FP32 pipes, "
+                 "~2^-48 relative)",
         "data": "synthetic (seeded iid N(0,1))",
         "config": {"workload": desc, "columns_per_gpu": M,
                    "parallelism": "replicas over columns (no collective)",
                    "l2": "inputs larger than L2 (%.0f MiB per operand)" %
                          (r64['bytes'] / 2 / 2 ** 20)},
+        "rel_err_vs_oracle": rel64,
+        "oracle_sample": "column 0",
         "fp32_form": {
             "value": world * r32['bytes'] / (r32['ms'] * 1e-3) / 1e9,
             "unit": "GB/s", "ms_per_step": r32['ms'],
             "speedup_vs_fp64": r64['ms'] / r32['ms'],
-            "rel_err_vs_fp64": rel, "dtype": "c64",
-            "roofline": roofline(r32, 'fp32')},
-        "roofline": roofline(r64, 'fp64'),
+            "rel_err_vs_oracle": rel32, "rel_err_vs_fp64": rel32_64,
+            "dtype": "c64", "roofline": r32['roofline']},
+        "roofline": r64['roofline'],
         "e2e": e2e,
         "gpu_launches": int(args.steps * r64['n_launch']),
-        "clocks": clk,
+        "clocks": r64['clk'],
     }
-    if args.workload == 'chain':
+    if name == 'chain':
         line["differentiable"] = measure_grad(torch, fg, args)
-    if args.workload == 'hadamard':
-        line["bf16_form"] = measure_bf16(torch, fg, args, build_fn, n_in, M,
-                                         xe, op64, peak, peak_kind)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.workload)
+        line["cpu_baseline"] = cpu_baseline(name)
+    if name == 'kron' and not args.only and world == 1:
+        del r64, r32
+        torch.cuda.empty_cache()
+        configs = {}
+        for key, fn, cpu in (('circulant', config_circulant, 'circulant'),
+                             ('hadamard', config_hadamard, 'hadamard'),
+                             ('chain', config_chain, 'chain'),
+                             ('batched', config_batched, 'batched')):
+            configs[key] = fn(torch, fg, args, ctx)
+            if not args.no_cpu_baseline:
+                configs[key]["cpu_baseline"] = cpu_baseline(cpu,
+                                                            budget_s=3.0)
+            torch.cuda.empty_cache()
+        line["configs"] = configs
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
-
-
-def measure_bf16(torch, fg, args, build_fn, n_in, M, xe, op64, peak,
-                 peak_kind):
-    """The tensor-core form of the Hadamard workload: float32 data, the
-    16-point groups as BF16 MMA with FP32 accumulation (three-term split)."""
-    op, _, _ = build_fn(fg, 'bf16')
-    dt = np.float32
-    if not args.no_autotune:
-        op.autotune(M, out_dtype=np.float32)
-    xt = torch.from_numpy(xe.astype(dt).T).cuda().t()
-    ms, yt = time_device(torch, op, xt, args.steps, args.warmup,
-                         lambda: None)
-    y64 = op64.forward(torch.from_numpy(xe.T).cuda().t()).cpu().numpy()
-    rel = float(np.max(np.abs(yt.cpu().numpy().astype(np.float64) - y64)) /
-                np.max(np.abs(y64)))
-    plan = op.plan(np.float32)
-    code = fg._native.DTYPE_CODE
-    n_out = op.numRows
-    launches = np.mean(np.array([plan.execute_profiled(
-        fg._native.FORWARD, xt.data_ptr(), code[np.dtype(dt)], n_in,
-        yt.data_ptr(), code[np.dtype(dt)], n_out, M,
-        torch.cuda.current_stream().cuda_stream) for _ in range(3)]), axis=0)
-    nbytes = (n_in + n_out) * M * 4
-    k = int(np.argmax(launches))
-    ach = nbytes / (launches[k] * 1e-3) / 1e9
-    return {"value": nbytes / (ms * 1e-3) / 1e9, "unit": "GB/s",
-            "ms_per_step": ms, "dtype": "f32 data, bf16 x3 MMA, f32 accum",
-            "rel_err_vs_fp64": rel,
-            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak,
-                         "unit": "GB/s", "frac": ach / peak,
-                         "traffic": ncu_traffic(args.workload, 'bf16', k + 1),
-                         "peak_kind": peak_kind,
-                         "kernel": "vprog launch %d of %d (tensor-core "
-                                   "FWHT groups)" % (k + 1, len(launches)),
-                         "launch_ms": [round(float(v), 4) for v in launches]}}
 
 
 def _time_events(torch, fn, steps, warmup):
@@ -516,108 +737,29 @@ def measure_grad(torch, fg, args):
 
 
 def run_batched(args):
-    """Many operators in one persistent launch (complex64), replayed as a
-    CUDA graph, against the plain FP64 path applying them one by one."""
+    """The batched configuration alone (its own JSON line)."""
     import torch
     rank, world, local = dist_info()
     barrier, allmax = _dist_setup(torch, world, local)
     import fastmat_gb300 as fg
-    specs = batched_specs(seed=rank)
-    ops32 = batched_ops(fg, specs, 'fp32')
-    ops64 = batched_ops(fg, specs)
-    rng = np.random.default_rng(100 + rank)
-    xs, xs64 = [], []
-    for op, m in ops32:
-        x = (rng.standard_normal((m, op.numCols)) +
-             1j * rng.standard_normal((m, op.numCols))).astype(np.complex64)
-        xs.append(torch.from_numpy(x).cuda().t())
-        xs64.append(xs[-1].to(torch.complex128))
-    nbytes = sum((op.numCols + op.numRows) * m * 8 for op, m in ops32)
-    batch = fg.Batch([(op, x) for (op, _), x in zip(ops32, xs)])
-    launches, levels, tiles = batch.info()
+    peak, peak_kind = measured_peak()
     dev = torch.cuda.current_device()
     uuid = getattr(torch.cuda.get_device_properties(dev), 'uuid', None)
     clocks = ClockSampler('GPU-%s' % uuid if uuid is not None else dev)
-    for _ in range(args.warmup):
-        batch.run(graph=True)
-    torch.cuda.synchronize()
-    barrier()
     clocks.start()
-    ms = _time_events(torch, lambda: batch.run(graph=True), args.steps, 0)
+    r = config_batched(torch, fg, args, (barrier, allmax, peak, peak_kind))
     clk = clocks.stop()
-    batch.check()
-    ms = allmax(ms)
-    ys = [y.clone() for y in batch.outputs]
-
-    def per_op64():
-        for (op, _), x in zip(ops64, xs64):
-            op.forward(x)
-
-    ms64 = allmax(_time_events(torch, per_op64, 2, 1))
-    rel = 0.0
-    for (op, _), x, y in zip(ops64, xs64, ys):
-        r = op.forward(x)
-        rel = max(rel, float((y.to(torch.complex128) - r).abs().max() /
-                             r.abs().max()))
-    # e2e: pinned host inputs / outputs, copies inside the timed region
-    hx = [x.t().contiguous().cpu().pin_memory() for x in xs]
-    hy = [torch.empty(tuple(y.t().shape), dtype=y.dtype).pin_memory()
-          for y in ys]
-    dx = [x.t() for x in xs]            # row-major (M, n) views of the inputs
-    dy = [y.t() for y in batch.outputs]
-
-    def e2e_step():
-        for h, d in zip(hx, dx):
-            d.copy_(h, non_blocking=True)
-        batch.run(graph=True)
-        for h, d in zip(hy, dy):
-            h.copy_(d, non_blocking=True)
-        torch.cuda.synchronize()
-
-    for _ in range(args.warmup):
-        e2e_step()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_ms = allmax((time.perf_counter() - t0) * 1e3 / args.steps)
-    peak, peak_kind = measured_peak()
-    achieved = nbytes / (ms * 1e-3) / 1e9
-    h2d = sum(op.numCols * m * 8 for op, m in ops32)
     line = {
         "metric": "matvec GB/s vs HBM roofline; FP32 vs FP64 GPU speedup at "
                   "rel err <=1e-5",
-        "value": world * achieved, "unit": "GB/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64", "data": "synthetic (seeded iid N(0,1))",
-        "config": {"workload": WORKLOADS['batched'][3],
-                   "operators": len(ops32),
-                   "plan_launches_replaced": launches, "levels": levels,
-                   "tiles": tiles,
-                   "parallelism": "replicas (each rank its own batch)",
-                   "l2": "working set %.0f MiB (larger than L2)" %
-                         (nbytes / 2 ** 20)},
-        "fp64_per_operator": {"ms_per_step": ms64,
-                              "value": world * nbytes * 2 / (ms64 * 1e-3) /
-                              1e9,
-                              "unit": "GB/s", "dtype": "c128",
-                              "speedup_of_batch": ms64 / ms,
-                              "rel_err_batch_vs_fp64": rel},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ncu_traffic('batched', 'fp32', 1),
-                     "peak_kind": peak_kind,
-                     "kernel": "batch_kernel (one cooperative launch)"},
-        "e2e": {"value": world * nbytes / (e2e_ms * 1e-3) / 1e9,
-                "unit": "GB/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(nbytes - h2d),
-                "path": "pinned host buffers, one copy per operand, graph "
-                        "replay of the batch"},
-        "gpu_launches": int(args.steps),
-        "clocks": clk,
-    }
+        "value": world * r['value'], "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r['ms_per_step'], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (seeded iid N(0,1))",
+        "config": {"workload": r['workload'], "operators": r['operators']},
+        "roofline": r['roofline'], "gpu_launches": int(args.steps),
+        "clocks": clk, "batched": r}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline('batched')
     if rank == 0:
@@ -860,6 +1002,9 @@ def main():
     ap.add_argument('--workload', default='kron', choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-autotune', action='store_true')
+    ap.add_argument('--only', action='store_true',
+                    help='the chosen workload alone (the default kron run '
+                         'also measures the other configurations)')
     ap.add_argument('--profile-target', type=int, default=0, metavar='COLS',
                     help='no timing: run the workload forward twice on COLS '
                          'columns with the tile shapes tuned for the full '
