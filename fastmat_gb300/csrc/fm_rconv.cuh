@@ -81,18 +81,48 @@ __host__ __device__ constexpr int rc_log2(int n) {
   return n <= 1 ? 0 : 1 + rc_log2(n / 2);
 }
 
-// shared-memory position of point p of a vector buffer: one spare point per
-// 128 bytes spreads strided butterfly accesses over the banks
-template <class E> __device__ __forceinline__ int rc_pad(int p) {
-  constexpr int SH = sizeof(E) == 8 ? 4 : 3;
-  return p + (p >> SH);
-}
+// Shared-memory layout of a vector's exchange buffer: point p at
+// p + (p >> SH), vectors Lp points apart; its input slot: natural order,
+// vectors Ls points apart.  (SH, Lp, Ls) per element size and length were
+// chosen by enumerating the bank pattern of every access the kernel makes
+// (the stage layouts' exchange writes and reads and the slot reads, per
+// half- or quarter-warp phase): all are conflict-free except the exchange
+// of L = 32 (4 wavefronts where 3 would do, on average); the twiddle and
+// spectrum tables are read lane-major (consecutive lanes, consecutive
+// entries) and broadcast across the vectors of a warp.
 template <class E, int L> struct RcBuf {
-  static constexpr int SH = sizeof(E) == 8 ? 4 : 3;
-  // padded length; the extra half-granule row shift makes consecutive
-  // vectors of a warp start on different banks
-  static constexpr int Lp = L + (L >> SH) + (L >= (1 << SH) ? 0 : 1);
+  static constexpr bool C64 = sizeof(E) == 8;
+  static constexpr int SH =
+      C64 ? (L == 64 ? 2 : L == 128 ? 3 : 4) : (L == 32 ? 2 : 3);
+  static constexpr int Lp =
+      C64 ? (L == 16 ? 17 : L == 32 ? 34 : L == 64 ? 84 : L == 128 ? 152
+             : L + (L >> 4))
+          : (L == 8 ? 9 : L == 32 ? 44 : L + (L >> 3));
+  // input slot stride (natural order, read at g + G r): conflict-free
+  static constexpr int Ls = C64 ? (L <= 128 ? L + L / 16 : L)
+                                : (L <= 32 ? L + L / 8 : L);
 };
+template <class E, int L> __device__ __forceinline__ int rc_pad(int p) {
+  return p + (p >> RcBuf<E, L>::SH);
+}
+
+// Offset of stage I's lane-major twiddle table (R_I x G entries, stages
+// with M > 1 only) within the twiddle area of shared memory.
+template <class E, int L, int I>
+__host__ __device__ constexpr int rc_twoff() {
+  constexpr int P = RcLane<E>::P;
+  if constexpr (I == 0) {
+    return 0;
+  } else {
+    constexpr int R = rc_radix(I - 1, L, P);
+    constexpr int M = rc_mprev(I - 1, L, P) / R;
+    return rc_twoff<E, L, I - 1>() + (M > 1 ? R * (L / P) : 0);
+  }
+}
+template <class E, int L, int I>
+__host__ __device__ constexpr int rc_twlen() {  // entries of stages < I
+  return rc_twoff<E, L, I>();
+}
 
 // Stage `I` of the forward (INV = false: DFT, then twiddles of the outputs)
 // or inverse (INV = true: conjugate twiddles of the inputs, then DFT with
@@ -109,13 +139,16 @@ __device__ __forceinline__ void rc_stage(E (&x)[RcLane<E>::P], int g,
   constexpr int TS = L / Mprev;  // table stride of w_Mprev
   constexpr int SG = INV ? +1 : -1;
   typedef typename Lazy<E>::type LC;
-  const int t = g & (M - 1);
-  // the twiddles w_Mprev^(t k), k < R, are the same for all u
+  constexpr int G = L / P;
+  // the twiddles w_Mprev^(t k), t = g mod M, k < R, are the same for all
+  // u: lane-major table of this stage (entry k G + g), conflict-free reads
   E w[R];
   if constexpr (M > 1) {
+    const E *tab = stw + rc_twoff<E, L, I>();
 #pragma unroll
-    for (int k = 1; k < R; ++k) w[k] = stw[t * k * TS];
+    for (int k = 1; k < R; ++k) w[k] = tab[k * G + g];
   }
+  (void)TS;
 #pragma unroll
   for (int u = 0; u < NB; ++u) {
     LC v[R];
@@ -163,10 +196,12 @@ __device__ __forceinline__ void rc_exchange(E (&x)[RcLane<E>::P], E *buf,
   constexpr int P = RcLane<E>::P;
   const int ba = rc_base<E, L, IA>(g), bb = rc_base<E, L, IB>(g);
 #pragma unroll
-  for (int j = 0; j < P; ++j) buf[rc_pad<E>(ba + rc_off<E, L, IA>(j))] = x[j];
+  for (int j = 0; j < P; ++j)
+    buf[rc_pad<E, L>(ba + rc_off<E, L, IA>(j))] = x[j];
   __syncwarp();
 #pragma unroll
-  for (int j = 0; j < P; ++j) x[j] = buf[rc_pad<E>(bb + rc_off<E, L, IB>(j))];
+  for (int j = 0; j < P; ++j)
+    x[j] = buf[rc_pad<E, L>(bb + rc_off<E, L, IB>(j))];
   __syncwarp();
 }
 
@@ -200,9 +235,33 @@ template <class E, int L> struct RcOcc {
 // (the next vectors, copied in ahead) and an exchange buffer
 template <class E, int L>
 __host__ __device__ constexpr size_t rc_smem() {
-  return (size_t)(2 * L + 2 * (FM_RC_THREADS / 32) *
-                              (32 / (L / RcLane<E>::P)) * RcBuf<E, L>::Lp) *
+  return (size_t)(rc_twlen<E, L, rc_stages(L, RcLane<E>::P)>() + L +
+                  (FM_RC_THREADS / 32) * (32 / (L / RcLane<E>::P)) *
+                      (RcBuf<E, L>::Lp + RcBuf<E, L>::Ls)) *
          sizeof(E);
+}
+
+// Fill the lane-major twiddle tables of stages I.. from the natural table
+// tw[j] = exp(-2 pi i j / L): entry k G + g of stage I is w_Mprev^(t k),
+// t = g mod M (the stage's table stride L / Mprev in tw).
+template <class E, int L, int I>
+__device__ __forceinline__ void rc_fill_tw(E *stw, const E *tw) {
+  constexpr int P = RcLane<E>::P;
+  constexpr int S = rc_stages(L, P);
+  if constexpr (I < S) {
+    constexpr int R = rc_radix(I, L, P);
+    constexpr int Mprev = rc_mprev(I, L, P);
+    constexpr int M = Mprev / R;
+    constexpr int G = L / P;
+    if constexpr (M > 1) {
+      E *tab = stw + rc_twoff<E, L, I>();
+      for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
+        const int k = i / G, g = i % G;
+        tab[i] = tw[(g & (M - 1)) * k * (L / Mprev)];
+      }
+    }
+    rc_fill_tw<E, L, I + 1>(stw, tw);
+  }
 }
 
 template <class E, int L>
@@ -215,19 +274,25 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
   constexpr int S = rc_stages(L, P);
   constexpr int Lp = RcBuf<E, L>::Lp;
   extern __shared__ __align__(128) unsigned char fm_smem[];
+  constexpr int TWN = rc_twlen<E, L, S>();
   E *stw = reinterpret_cast<E *>(fm_smem);
-  E *sspec = stw + L;
+  E *sspec = stw + TWN;
   E *sx = sspec + L;
+  rc_fill_tw<E, L, 0>(stw, (const E *)p.tw);
+  // spectrum in lane-major order: entry j G + g is the point lane g holds
+  // in register j after the last forward stage
   for (int i = threadIdx.x; i < L; i += blockDim.x) {
-    stw[i] = ((const E *)p.tw)[i];
-    sspec[i] = ((const E *)p.spec)[i];
+    const int j = i / G, gg = i % G;
+    sspec[i] = ((const E *)p.spec)[rc_base<E, L, S - 1>(gg) +
+                                    rc_off<E, L, S - 1>(j)];
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int q = lane / G, g = lane % G;
   E *buf = sx + (wib * VPW + q) * Lp;  // exchange buffer of this vector
   // input slot of this vector: the raw bits of its points, natural order
-  E *slot = sx + ((FM_RC_THREADS / 32) + wib) * VPW * Lp + q * Lp;
+  E *slot = sx + (FM_RC_THREADS / 32) * VPW * Lp +
+            (wib * VPW + q) * RcBuf<E, L>::Ls;
   const i64 NV = p.A * p.num_cols;
   const FDiv dA((unsigned)p.A);
   const i64 nwarps = (i64)gridDim.x * (blockDim.x >> 5);
@@ -334,13 +399,9 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
     }
     // ---- forward transform, spectrum product, inverse transform
     rc_forward<E, L, 0>(x, buf, g, stw);
-    {
-      const int bs = rc_base<E, L, S - 1>(g);
 #pragma unroll
-      for (int j = 0; j < P; ++j)
-        x[j] = mulv(x[j], sspec[bs + rc_off<E, L, S - 1>(j)],
-                    p.spec_conj != 0);
-    }
+    for (int j = 0; j < P; ++j)
+      x[j] = mulv(x[j], sspec[j * G + g], p.spec_conj != 0);
     rc_inverse<E, L, S - 1>(x, buf, g, stw);
     // ---- store points g + G r
     if (act) {
