@@ -301,6 +301,8 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
   // converted by synchronous loads
   const bool raw_in = p.src_type == Tr<E>::code;
   const bool raw_out = p.dst_type == Tr<E>::code && !p.accumulate;
+  const bool plain_out =
+      raw_out && !p.post && !p.has_scale && !p.conj_out;
   const E cs = scalar_of<E>(p.scale_re, p.scale_im);
   typedef typename std::conditional<Emu<E>::v, double2, E>::type Raw;
   static_assert(sizeof(Raw) == sizeof(E), "raw element size");
@@ -315,12 +317,18 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
     const Raw *src = (const Raw *)p.src + (i64)m * p.ld_src +
                      (i64)a * p.in_stride;
     const i64 left = p.in_rows - (i64)a * p.in_stride;
+    if (act && p.in_len == L && left >= L) {  // whole vector: no masks
 #pragma unroll
-    for (int r = 0; r < P; ++r) {
-      const int j = g + G * r;
-      const bool ok = act && j < p.in_len && j < left;
-      cp_async<sizeof(E)>(slot + j, ok ? (const void *)(src + j)
-                                       : (const void *)p.src, ok);
+      for (int r = 0; r < P; ++r)
+        cp_async<sizeof(E)>(slot + g + G * r, src + g + G * r, true);
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const int j = g + G * r;
+        const bool ok = act && j < p.in_len && j < left;
+        cp_async<sizeof(E)>(slot + j, ok ? (const void *)(src + j)
+                                         : (const void *)p.src, ok);
+      }
     }
     cp_async_commit();
   };
@@ -404,7 +412,18 @@ __global__ void __launch_bounds__(FM_RC_THREADS, (RcOcc<E, L>::v))
       x[j] = mulv(x[j], sspec[j * G + g], p.spec_conj != 0);
     rc_inverse<E, L, S - 1>(x, buf, g, stw);
     // ---- store points g + G r
-    if (act) {
+    if (act && plain_out && p.out_len == L && rout0 + L <= p.out_rows) {
+      // whole vector in the buffer's type, nothing applied on the way out
+      const i64 base = (i64)m * p.ld_dst + rout0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        if constexpr (Emu<E>::v)
+          ((double2 *)p.dst)[base + g + G * r] = make_double2(
+              df2d_scaled(x[r].x, sexp), df2d_scaled(x[r].y, sexp));
+        else
+          ((E *)p.dst)[base + g + G * r] = x[r];
+      }
+    } else if (act) {
 #pragma unroll
       for (int r = 0; r < P; ++r) {
         const int j = g + G * r;
