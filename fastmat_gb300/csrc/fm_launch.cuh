@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "fm_rconv.cuh"
+#include "fm_rfwht.cuh"
 #include "fm_vprog.cuh"
 
 namespace fmk {
@@ -62,6 +63,12 @@ cudaError_t launch_spmv(int ctype, const SpStep &p, int group,
 int rconv_max_len(int ctype);
 int rconv_min_len(int ctype);
 cudaError_t launch_rconv(int ctype, const RcStep &p, cudaStream_t s);
+
+// register-resident FWHT of contiguous real vectors (fm_rfwht.cuh):
+// lengths it is built for (powers of two; 0: not for this type), one launch
+int rfwht_min_len(int ctype);
+int rfwht_max_len(int ctype);
+cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s);
 
 // largest FFT radix the kernels of a compute type are built with (see
 // MinBlocks / Radix16 in fm_vprog.cuh): 8 for single precision and

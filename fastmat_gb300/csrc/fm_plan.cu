@@ -233,8 +233,9 @@ struct LStep {
   // first row of the launch's operand inside its buffer (Blocks segments)
   i64 src_off = 0, dst_off = 0;
   // 0: vector program (vprog_kernel); 1: CSR sparse product (spmv_kernel);
-  // 2: register-resident convolution (rconv_kernel), whose `st` still holds
-  // the equivalent vector program (run by batches)
+  // 2: register-resident convolution (rconv_kernel), 3: register-resident
+  // FWHT (rfwht_kernel); for both `st` still holds the equivalent vector
+  // program (run by batches, and by kind 3 when the buffers do not suit it)
   int kind = 0;
   int rc_L = 0;
   const void *rc_spec = nullptr, *rc_tw = nullptr;  // spectrum in rconv order
@@ -1566,9 +1567,32 @@ class Planner {
     ls.kind = 2;
   }
 
+  // A program that is one FWHT over contiguous whole vectors of real data,
+  // with a length the register FWHT is built for, runs there (kind 3).
+  void try_rfwht(LStep &ls, const std::vector<fmk::Op> &ops) {
+    const int ct = P_->ctype;
+    const fmk::Step &st = ls.st;
+    const int lmin = fmk::rfwht_min_len(ct), lmax = fmk::rfwht_max_len(ct);
+    if (!lmax || ops.size() != 1 || ops[0].kind != fmk::OP_FWHT ||
+        ops[0].sign != 0)
+      return;
+    const int L = ops[0].len;
+    if (!is_pow2(L) || L < lmin || L > lmax || st.L != L) return;
+    if (st.vin.Cc != 1 || st.vout.Cc != 1 || st.vin.n != L ||
+        st.vout.n != L || st.vin.A != st.vout.A || st.in_len != L ||
+        st.out_len != L || st.in_rows != st.vin.A * L ||
+        st.out_rows != st.vout.A * L || st.map_in || st.map_out ||
+        st.out_mode || st.pre || st.post || st.conj_in || st.conj_out ||
+        st.has_scale || st.accumulate)
+      return;
+    ls.rc_L = L;
+    ls.kind = 3;
+  }
+
   void finish(LStep &ls, const std::vector<fmk::Op> &ops_in) {
     fmk::Step &st = ls.st;
     try_rconv(ls, ops_in);
+    if (ls.kind == 0) try_rfwht(ls, ops_in);
     std::vector<fmk::Op> ops = ops_in;
     st.out_pos = finalize(ops);
     if ((int)ops.size() > FM_MAX_OPS)
@@ -1983,6 +2007,32 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 
 // Finish a bound launch (TMA descriptors, status word) and issue it.
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
+  if (ls.kind == 3) {
+    // raw buffers of the I/O type, 16-byte aligned columns and vectors
+    const int esz = esize(P->io_type);
+    const bool fit = st.src_type == P->io_type && st.dst_type == P->io_type &&
+                     ((uintptr_t)st.src & 15) == 0 &&
+                     ((uintptr_t)st.dst & 15) == 0 &&
+                     (st.ld_src * esz) % 16 == 0 &&
+                     (st.ld_dst * esz) % 16 == 0 && !st.accumulate;
+    if (fit) {
+      fmk::RfStep rf;
+      rf.src = st.src;
+      rf.dst = st.dst;
+      rf.ld_src = st.ld_src;
+      rf.ld_dst = st.ld_dst;
+      rf.A = st.vin.A;
+      rf.stride = st.vin.n;
+      rf.num_cols = st.num_cols;
+      rf.err = P->err;
+      rf.L = ls.rc_L;
+      if (rf.A * rf.num_cols >= 0x7fffffffLL)
+        fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
+      CUDA_TRY(fmk::launch_rfwht(P->ctype, rf, s));
+      return;
+    }
+    // otherwise the equivalent vector program below
+  }
   if (ls.kind == 2) {
     fmk::RcStep rc;
     memset(&rc, 0, sizeof(rc));
@@ -2783,6 +2833,15 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
         s += line;
         continue;
       }
+      if (ls.kind == 3) {
+        snprintf(line, sizeof(line),
+                 "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,"
+                 "%lld) rfwht L=%d acc=%d: fwht(%d)\n",
+                 ls.src, ls.dst, st.vin.A, st.vin.n, st.vin.Cc, st.vout.A,
+                 st.vout.n, st.vout.Cc, ls.rc_L, st.accumulate, ls.rc_L);
+        s += line;
+        continue;
+      }
       if (ls.kind == 2) {
         snprintf(line, sizeof(line),
                  "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,"
@@ -2900,6 +2959,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
         if (ls0.kind == 1)
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: sparse operators run "
                                    "outside batches");
+        // (register convolutions and FWHTs run as their vector program)
         LStep ls = ls0;  // register convolutions run as their vector program
         if (!configure(esz, ls, 0, 0, false, 0, false))
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "

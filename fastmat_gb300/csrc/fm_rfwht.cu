@@ -1,0 +1,83 @@
+// Instantiations and launcher of the register-resident FWHT kernel
+// (fm_rfwht.cuh): float32 and double-float real data, contiguous vectors of
+// 1024..8192 (float32) or 256..8192 (double-float) points.
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "../../include/fmgpu.h"
+#include "fm_launch.cuh"
+#include "fm_rfwht.cuh"
+
+namespace fmk {
+
+namespace {
+
+template <class E, int L>
+cudaError_t launch_one(const RfStep &p, cudaStream_t s) {
+  auto *fn = rfwht_kernel<E, L>;
+  constexpr size_t smem = rf_smem<E, L>();
+  constexpr int T = RfShape<E, L>::T, VPC = RfShape<E, L>::VPC;
+  static std::mutex mu;
+  static std::map<int, int> resident;  // device -> CTAs per SM x SMs
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int cap = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find(dev);
+    if (it == resident.end()) {
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, sms = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      it = resident.emplace(dev, (per_sm < 1 ? 1 : per_sm) * sms).first;
+    }
+    cap = it->second;
+  }
+  const long long nv = (long long)p.A * p.num_cols;
+  long long grid = (nv + VPC - 1) / VPC;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  fn<<<(unsigned)grid, T, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int rfwht_min_len(int ctype) {
+  return ctype == FM_F32 ? 1024 : ctype == FM_F64_DF ? 256 : 0;
+}
+int rfwht_max_len(int ctype) {
+  return ctype == FM_F32 || ctype == FM_F64_DF ? 8192 : 0;
+}
+
+cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s) {
+  if (ctype == FM_F32) {
+    switch (p.L) {
+      case 1024: return launch_one<float, 1024>(p, s);
+      case 2048: return launch_one<float, 2048>(p, s);
+      case 4096: return launch_one<float, 4096>(p, s);
+      case 8192: return launch_one<float, 8192>(p, s);
+      default: break;
+    }
+  } else if (ctype == FM_F64_DF) {
+    switch (p.L) {
+      case 256: return launch_one<df, 256>(p, s);
+      case 512: return launch_one<df, 512>(p, s);
+      case 1024: return launch_one<df, 1024>(p, s);
+      case 2048: return launch_one<df, 2048>(p, s);
+      case 4096: return launch_one<df, 4096>(p, s);
+      case 8192: return launch_one<df, 8192>(p, s);
+      default: break;
+    }
+  }
+  return cudaErrorInvalidConfiguration;
+}
+
+}  // namespace fmk

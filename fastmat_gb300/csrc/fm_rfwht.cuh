@@ -1,0 +1,264 @@
+// Register-resident Walsh-Hadamard transform of contiguous power-of-two
+// vectors (fastmat's Hadamard, fastmat/Hadamard.pyx:164-230: a + b / a - b
+// butterflies at distance 1, 2, 4, ...), for real float32 and double-float
+// data.
+//
+//   * a vector of L points is held by G = L / P threads of a CTA, P points
+//     per thread (32 float or 16 double-float); the CTA works on
+//     max(1, 256 / G) vectors at a time;
+//   * the index bits are taken in passes of log2(P) bits from the least
+//     significant one, so the butterflies run in fastmat's order and float32
+//     results are bit-identical to its float32 transform; within a pass every
+//     thread's groups of points (the points that differ only in the pass's
+//     bits) are in its registers, and the levels of the pass are plain
+//     register butterflies (double-float: unnormalised inside the pass, one
+//     renormalisation at its end);
+//   * the first pass takes thread t's P consecutive points (t P .. t P + P-1)
+//     from a shared-memory slot that cp.async filled one batch ahead; between
+//     passes the points go through a shared-memory exchange buffer (CTA
+//     barriers: a long vector spans several warps); the last pass stores
+//     straight to global memory, consecutive threads on consecutive points.
+//
+// Thread t's groups at a pass with bit offset s and width w are
+// h = t + G u (u < P / 2^w); point r of group h sits at
+// ((h >> s) << (s + w)) | (r << s) | (h mod 2^s).  The exchange buffer puts
+// point e at e + (e >> 5) (float) or e + (e >> 4) (double-float), the slot
+// holds raw float32 / float64 words with a 16-byte pad per 128 bytes: every
+// access pattern of the kernel is then free of bank conflicts (checked by
+// enumerating them for the lengths instantiated).
+#pragma once
+
+#include <type_traits>
+
+#include "fm_vprog.cuh"
+
+namespace fmk {
+
+// One launch of the register FWHT (built by the planner from a vector
+// program that is one FWHT over contiguous whole vectors).
+struct RfStep {
+  const void *src;
+  void *dst;
+  i64 ld_src, ld_dst;
+  i64 A;       // vectors per column
+  i64 stride;  // rows from one vector of a column to the next
+  i64 num_cols;
+  int *err;
+  int L;
+};
+
+#define FM_RF_THREADS 256
+template <class E> struct RfLane {
+  static constexpr int P = std::is_same<E, float>::value ? 32 : 16;
+  static constexpr int PB = std::is_same<E, float>::value ? 5 : 4;
+  // raw word of the global buffers: float32 or float64
+  typedef typename std::conditional<std::is_same<E, float>::value, float,
+                                    double>::type Raw;
+  static constexpr int XSH = std::is_same<E, float>::value ? 5 : 4;
+};
+template <class E, int L> struct RfShape {
+  static constexpr int P = RfLane<E>::P;
+  static constexpr int G = L / P;
+  static constexpr int T = G > FM_RF_THREADS ? G : FM_RF_THREADS;
+  static constexpr int VPC = T / G;  // vectors per CTA batch
+  typedef typename RfLane<E>::Raw Raw;
+  static constexpr int CH = 16 / (int)sizeof(Raw);   // raw words per chunk
+  static constexpr int ROW = 128 / (int)sizeof(Raw);  // raw words per 128 B
+  static constexpr int Ls = L + (L / ROW) * CH;        // slot stride
+  static constexpr int Lx = L + (L >> RfLane<E>::XSH);  // exchange stride
+};
+__host__ __device__ constexpr int rf_log2(int n) {
+  return n <= 1 ? 0 : 1 + rf_log2(n / 2);
+}
+template <class E, int L>
+__host__ __device__ constexpr size_t rf_smem() {
+  typedef RfShape<E, L> S;
+  return (size_t)S::VPC * S::Ls * sizeof(typename S::Raw) +
+         (size_t)S::VPC * S::Lx * sizeof(E) + 64;
+}
+template <class E, int L> struct RfOcc {
+  static constexpr int v = RfShape<E, L>::T > 256 ? 1 : 2;
+};
+
+template <class E>
+__device__ __forceinline__ int rf_xpad(int e) {
+  return e + (e >> RfLane<E>::XSH);
+}
+__device__ __forceinline__ int rf_pos(int h, int s, int r, int w) {
+  return ((h >> s) << (s + w)) | (r << s) | (h & ((1 << s) - 1));
+}
+
+// the levels of one pass (w bits) on the thread's P registers, in place:
+// register u 2^w + r is point r of group u
+template <class LE, int P, int W>
+__device__ __forceinline__ void rf_levels(LE (&v)[P]) {
+  constexpr int R = 1 << W;
+#pragma unroll
+  for (int u = 0; u < P / R; ++u) {
+#pragma unroll
+    for (int h = 1; h < R; h <<= 1) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if ((r & h) == 0) {
+          const LE a = v[u * R + r], c = v[u * R + r + h];
+          v[u * R + r] = addv(a, c);
+          v[u * R + r + h] = subv(a, c);
+        }
+      }
+    }
+  }
+}
+
+template <class E, int L, int S0>
+__device__ __forceinline__ void rf_pass(E (&x)[RfLane<E>::P]) {
+  constexpr int P = RfLane<E>::P, PB = RfLane<E>::PB, K = rf_log2(L);
+  constexpr int W = K - S0 < PB ? K - S0 : PB;
+  typedef typename Lazy<E>::type LE;
+  LE v[P];
+#pragma unroll
+  for (int j = 0; j < P; ++j) v[j] = to_lazy(x[j]);
+  rf_levels<LE, P, W>(v);
+#pragma unroll
+  for (int j = 0; j < P; ++j) x[j] = from_lazy(v[j]);
+}
+
+// registers laid out for the pass at bit offset SA -> exchange buffer ->
+// registers for the pass at SB (CTA barriers)
+template <class E, int L, int SA, int SB>
+__device__ __forceinline__ void rf_exchange(E (&x)[RfLane<E>::P], E *buf,
+                                            int t) {
+  constexpr int P = RfLane<E>::P, PB = RfLane<E>::PB, K = rf_log2(L);
+  constexpr int G = L / P;
+  constexpr int WA = K - SA < PB ? K - SA : PB;
+  constexpr int WB = K - SB < PB ? K - SB : PB;
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+    const int u = j >> WA, r = j & ((1 << WA) - 1);
+    buf[rf_xpad<E>(rf_pos(t + G * u, SA, r, WA))] = x[j];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+    const int u = j >> WB, r = j & ((1 << WB) - 1);
+    x[j] = buf[rf_xpad<E>(rf_pos(t + G * u, SB, r, WB))];
+  }
+  __syncthreads();
+}
+
+template <class E, int L, int S0>
+__device__ __forceinline__ void rf_passes(E (&x)[RfLane<E>::P], E *buf,
+                                          int t) {
+  constexpr int PB = RfLane<E>::PB, K = rf_log2(L);
+  rf_pass<E, L, S0>(x);
+  if constexpr (S0 + PB < K) {
+    rf_exchange<E, L, S0, S0 + PB>(x, buf, t);
+    rf_passes<E, L, S0 + PB>(x, buf, t);
+  }
+}
+// bit offset of the last pass
+template <class E, int L> __host__ __device__ constexpr int rf_last() {
+  return ((rf_log2(L) - 1) / RfLane<E>::PB) * RfLane<E>::PB;
+}
+
+template <class E, int L>
+__global__ void __launch_bounds__(RfShape<E, L>::T, (RfOcc<E, L>::v))
+    rfwht_kernel(const __grid_constant__ RfStep p) {
+  typedef RfShape<E, L> Sh;
+  typedef typename Sh::Raw Raw;
+  constexpr int P = Sh::P, G = Sh::G, VPC = Sh::VPC;
+  constexpr int SL = rf_last<E, L>();
+  constexpr int WL = rf_log2(L) - SL;
+  extern __shared__ __align__(128) unsigned char fm_smem[];
+  Raw *slot = reinterpret_cast<Raw *>(fm_smem);
+  E *xb = reinterpret_cast<E *>(fm_smem + (size_t)VPC * Sh::Ls * sizeof(Raw));
+  int *sexp = reinterpret_cast<int *>(xb + (size_t)VPC * Sh::Lx);
+  const int vl = threadIdx.x / G, t = threadIdx.x % G;
+  Raw *vslot = slot + vl * Sh::Ls;
+  E *buf = xb + vl * Sh::Lx;
+  const i64 NV = p.A * p.num_cols;
+  const FDiv dA((unsigned)p.A);
+  const i64 step = (i64)gridDim.x * VPC;
+  // cp.async of a batch of VPC vectors into the slot, 16-byte chunks
+  auto prefetch = [&](i64 vb) {
+    constexpr int NCH = VPC * L / Sh::CH;
+    for (int c = threadIdx.x; c < NCH; c += Sh::T) {
+      const int v = c / (L / Sh::CH), ch = c % (L / Sh::CH);
+      const i64 gv = vb + v;
+      const bool ok = gv < NV;
+      const Raw *src = (const Raw *)p.src;
+      if (ok) {
+        const unsigned m = dA.div((unsigned)gv);
+        const unsigned a = (unsigned)gv - m * (unsigned)p.A;
+        src += (i64)m * p.ld_src + (i64)a * p.stride + (i64)ch * Sh::CH;
+      }
+      const int e = ch * Sh::CH;
+      cp_async<16>(slot + v * Sh::Ls + e + (e / Sh::ROW) * Sh::CH, src, ok);
+    }
+    cp_async_commit();
+  };
+  const i64 v0 = (i64)blockIdx.x * VPC;
+  if (v0 < NV) prefetch(v0);
+  for (i64 vb = v0; vb < NV; vb += step) {
+    const i64 gv = vb + vl;
+    const bool act = gv < NV;
+    cp_async_wait<0>();
+    __syncthreads();
+    // first pass: points t P .. t P + P - 1 of the vector
+    // (P raw words = 128 bytes per thread, one 16-byte pad after them)
+    Raw d[P];
+    {
+      typedef typename std::conditional<std::is_same<Raw, float>::value,
+                                        float4, double2>::type V;
+      const V *src = reinterpret_cast<const V *>(vslot + t * (P + Sh::CH));
+#pragma unroll
+      for (int c = 0; c < P / Sh::CH; ++c)
+        *reinterpret_cast<V *>(d + c * Sh::CH) = src[c];
+    }
+    __syncthreads();
+    if (vb + step < NV) prefetch(vb + step);
+    E x[P];
+    int s = 0;
+    if constexpr (Emu<E>::v) {
+      // double-float: every vector scaled by the power of two of its
+      // largest exponent (float's exponent range), restored on store
+      // (reduced over the vector's lanes within each warp, then across its
+      // warps in shared memory)
+      constexpr int WV = G < 32 ? G : 32;
+      int emax = 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) emax = max(emax, dexp(d[r]));
+#pragma unroll
+      for (int o = WV / 2; o >= 1; o /= 2)
+        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o, WV));
+      if (threadIdx.x < VPC) sexp[threadIdx.x] = 0;
+      __syncthreads();
+      if (t % WV == 0 && emax > 0) atomicMax(sexp + vl, emax);
+      __syncthreads();
+      s = sexp[vl] > 0 ? sexp[vl] - 1023 : 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) x[r] = d2df_scaled(d[r], s);
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; ++r) x[r] = d[r];
+    }
+    rf_passes<E, L, 0>(x, buf, t);
+    // last pass's points, straight to global memory
+    if (act) {
+      const unsigned m = dA.div((unsigned)gv);
+      const unsigned a = (unsigned)gv - m * (unsigned)p.A;
+      Raw *dst = (Raw *)p.dst + (i64)m * p.ld_dst + (i64)a * p.stride;
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+        const int u = j >> WL, r = j & ((1 << WL) - 1);
+        const int e = rf_pos(t + G * u, SL, r, WL);
+        if constexpr (Emu<E>::v)
+          dst[e] = df2d_scaled(x[j], s);
+        else
+          dst[e] = x[j];
+      }
+    }
+  }
+  cp_async_wait<0>();
+}
+
+}  // namespace fmk

@@ -189,3 +189,24 @@ def test_hadamard_order22_float32_bit_exact_columns():
     y = fg.Hadamard(22).forward(x)
     pick = [0, 21, 42, 63]
     _same(y[:, pick], fo.Hadamard(22).forward(np.asfortranarray(x[:, pick])))
+
+
+@pytest.mark.parametrize('order', [10, 12, 13])
+def test_hadamard_float32_unaligned_columns_bit_exact(order):
+    """Columns with a leading dimension that breaks 16-byte alignment run
+    the FWHT through the stage kernel instead of the register kernel: the
+    same butterflies in the same order, so the same bits."""
+    import torch
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(order + 100)
+    n = 1 << order
+    big = torch.from_numpy(rng.standard_normal((3, n + 1)).astype(
+        np.float32)).cuda()
+    xt = big[:, :n].t()                  # leading dimension n + 1
+    H = fg.Hadamard(order)
+    y = H.forward(xt).cpu().numpy()
+    x = xt.cpu().numpy()
+    _same(y, fo.Hadamard(order).forward(np.asfortranarray(x)))
+    # and the aligned call agrees bit for bit
+    ya = H.forward(torch.from_numpy(np.ascontiguousarray(x.T)).cuda().t())
+    _same(ya.cpu().numpy(), y)
