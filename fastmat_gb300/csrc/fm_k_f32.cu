@@ -16,6 +16,8 @@ KFn pick_main(int cls, int lay) {
     case 10: return vprog_kernel<float, 3, 1>;
     case 12: return vprog_kernel<float, 4, 0>;
     case 13: return vprog_kernel<float, 4, 1>;
+    case 18: return vprog_kernel<float, 6, 0>;
+    case 19: return vprog_kernel<float, 6, 1>;
     default: return nullptr;
   }
 }

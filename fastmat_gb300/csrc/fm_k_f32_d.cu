@@ -9,6 +9,7 @@ KFn pick_f32_dense(int cls) {
     case 0: return vprog_kernel<float, 0, 2>;
     case 3: return vprog_kernel<float, 3, 2>;
     case 4: return vprog_kernel<float, 4, 2>;
+    case 6: return vprog_kernel<float, 6, 2>;
     default: return nullptr;
   }
 }

@@ -373,8 +373,13 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   const int ept = ls.ept;
   // the tensor-core FWHT (class 4) works on whole warpgroups and needs
   // its staging area and TMEM bookkeeping beyond the tile ring
-  const int tgran = ls.cls == 4 ? 128 : 32;
-  const size_t extra = ls.cls == 4 ? (size_t)fmk::kTcBytes + 1024 : 0;
+  // (class 6: the tensor-core dense factor, the same granularity and its
+  // factor and row staging)
+  const bool tcg = ls.cls == 4 || ls.cls == 6;
+  const int tgran = tcg ? 128 : 32;
+  const size_t extra = ls.cls == 4   ? (size_t)fmk::kTcBytes + 1024
+                       : ls.cls == 6 ? (size_t)fmk::kTdBytes + 1024
+                                     : 0;
   auto threads_for = [&](int b) {
     i64 t = ((i64)b * L + ept - 1) / ept;
     t = (t + tgran - 1) / tgran * tgran;
@@ -396,13 +401,14 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   // element-major tiles: strided input and output views whose inner extent
   // holds whole tiles (B | Cc); rows of B * esz bytes (128 B when the thread
   // budget allows, never below 16 B), moved by TMA boxes
-  const bool em_class =
-      ls.cls == 1 || ls.cls == 3 || ls.cls == 4 || ls.cls == 5;
+  const bool em_class = ls.cls == 1 || ls.cls == 3 || ls.cls == 4 ||
+                        ls.cls == 5 || ls.cls == 6;
   if (want_lay == 1 && !(allow_em && em_class)) return false;
   if (allow_em && (want_lay == -1 || want_lay == 1) && em_class &&
       st.vin.Cc > 1 &&
       st.vout.Cc > 1) {
-    int B = want_B ? want_B : 128 / esz;
+    // (the tensor-core dense factor fills 128-row MMA chunks: 128 vectors)
+    int B = want_B ? want_B : (ls.cls == 6 ? 128 : 128 / esz);
     if (!want_B) {
       while (B > 1 && (st.vin.Cc % B || st.vout.Cc % B)) B /= 2;
       while (B * esz > 16 && threads_for(B) > FM_MAX_THREADS) B /= 2;
@@ -1279,6 +1285,9 @@ class Planner {
         fmk::Op o = mkop(fmk::OP_DENSE, (int)n_out);
         o.len2 = (int)n_in;
         o.ptr = upload(m);
+        // square factors of order <= 64 on float32 data in the tensor-core
+        // form run as MMA tiles (kernel class 6)
+        o.sign = P_->ctype == FM_F32_TC && R == C && R <= fmk::kTdMaxN;
         c.push_back(prog({o}, n_in, n_out, std::max(n_in, n_out)));
         return c;
       }
@@ -1432,7 +1441,12 @@ class Planner {
 
   int kernel_class(const std::vector<fmk::Op> &ops) {
     bool fft = false, odd = false, fwht = false, gen = false;
+    int dense = 0, dense_tc = 0;
     for (const fmk::Op &o : ops) {
+      if (o.kind == fmk::OP_DENSE) {
+        ++dense;
+        if (o.sign) ++dense_tc;
+      }
       if (o.kind == fmk::OP_FFT || o.kind == fmk::OP_DIF ||
           o.kind == fmk::OP_DIT) {
         fft = true;
@@ -1442,6 +1456,14 @@ class Planner {
       if (o.kind == fmk::OP_FWHT) fwht = true;
       if (o.kind == fmk::OP_GATHER || o.kind == fmk::OP_DENSE) gen = true;
     }
+    // one tensor-core dense factor with pointwise work around it
+    bool other = false;
+    for (const fmk::Op &o : ops)
+      if (o.kind == fmk::OP_GATHER || o.kind == fmk::OP_FFT ||
+          o.kind == fmk::OP_DIF || o.kind == fmk::OP_DIT ||
+          o.kind == fmk::OP_FWHT || o.kind == fmk::OP_ZPAD)
+        other = true;
+    if (dense == 1 && dense_tc == 1 && !other) return 6;
     if (gen || (fft && fwht)) return 0;
     if (fwht) return P_->ctype == FM_F32_TC ? 4 : 3;
     if (fft) return odd ? 2 : 1;

@@ -417,6 +417,7 @@ __device__ __forceinline__ E *vbase(E *sm, int b, int Lp) {
 
 }  // namespace fmk
 #include "fm_tc.cuh"
+#include "fm_tcdense.cuh"
 namespace fmk {
 
 // ------------------------------------------------------------ FFT stages
@@ -584,7 +585,7 @@ __device__ __forceinline__ void fft_stage(C *sm, int Lp, int B, int Lf,
 template <class E, int CLS> struct MinBlocks {
   static constexpr int v = ((std::is_same<E, float>::value ||
                              std::is_same<E, float2>::value) &&
-                            CLS != 4)
+                            CLS != 4 && CLS != 6)
                                ? 2
                                : 1;
 };
@@ -1508,7 +1509,8 @@ template <class E, int CLS, int LAY>
 __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
                                             int B, const VInfo *vi, i64 *sq,
                                             int tid, int T,
-                                            TcState *tc = nullptr) {
+                                            TcState *tc = nullptr,
+                                            TdState *td = nullptr) {
   for (int o = 0; o < p.nops; ++o) {
     const Op &op = p.ops[o];
     switch (op.kind) {
@@ -1543,6 +1545,8 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
       case OP_DENSE:
         if constexpr (CLS == 0 && LAY != 1)
           run_dense<E, LAY>(op, sm, Lp, B, tid, T);
+        if constexpr (CLS == 6 && std::is_same<E, float>::value)
+          run_densetc<LAY>(sm, Lp, B, *td, tid, T);
         break;
       case OP_ZPAD: run_zpad<E, LAY>(op, sm, Lp, B, tid, T); break;
       default:
@@ -1580,7 +1584,7 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
 // program's stages need warp barriers only.
 template <class E, int CLS, int LAY>
 __device__ __forceinline__ bool warp_mode(int B, int L, int nwarps) {
-  return LAY != 1 && CLS != 4 && nwarps > 1 && B % nwarps == 0 &&
+  return LAY != 1 && CLS != 4 && CLS != 6 && nwarps > 1 && B % nwarps == 0 &&
          (B / nwarps) * L <= 32 * Ept<E>::v;
 }
 
@@ -1625,6 +1629,17 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
         (launch_smem(B, Lp, sizeof(E), NB) + 1023) & ~(size_t)1023;
     tc_init(tcs, fm_smem + off, p.err, tid);
     tc = &tcs;
+  }
+  // class 6: the program's one dense factor, staged for the tensor cores
+  TdState tds;
+  if constexpr (CLS == 6 && std::is_same<E, float>::value) {
+    const size_t off =
+        (launch_smem(B, Lp, sizeof(E), NB) + 1023) & ~(size_t)1023;
+    const Op *dop = nullptr;
+    for (int o = 0; o < p.nops; ++o)
+      if (p.ops[o].kind == OP_DENSE) dop = &p.ops[o];
+    td_init(tds, fm_smem + off, (const float *)dop->ptr, dop->len, T, p.err,
+            tid);
   }
 
   i64 tile = blockIdx.x;
@@ -1702,10 +1717,10 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       // each warp runs the program on its own B / nwarps vectors
       const int w = tid >> 5, vw = B / nwarps;
       run_program<E, CLS, LAY>(p, sm + w * vw * Lp, Lp, vw, vi + w * vw,
-                               sq + w * vw, tid & 31, 32, tc);
+                               sq + w * vw, tid & 31, 32, tc, &tds);
       __syncthreads();
     } else {
-      run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc);
+      run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc, &tds);
     }
 
     if (tma_out) {
@@ -1762,6 +1777,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
   if (tma_out) bulk_wait_all();
   if (!tma_in) cp_async_wait<0>();
   if constexpr (CLS == 4) tc_release(tcs, tid);
+  if constexpr (CLS == 6 && std::is_same<E, float>::value)
+    td_release(tds, tid);
 }
 
 
