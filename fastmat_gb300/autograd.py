@@ -193,12 +193,24 @@ def _reduce(u, v, pre, n, post, d=None, w=None):
     return out
 
 
+def _tuned(op, x):
+    """Tile shapes of op's plan tuned for x's column count (once per
+    operator and column count; the choice is cached in memory and on
+    disk), as the plain operators are when their caller autotunes."""
+    cols = 1 if x.dim() == 1 else x.shape[1]
+    key = (cols, x.dtype)
+    if getattr(op, '_grad_tuned', None) != key:
+        op.autotune(cols, out_dtype=op._output_dtype(_numpy_dtype(x.dtype)))
+        op._grad_tuned = key
+    return op
+
+
 def _fwd(op, x):
-    return op.forward(x)
+    return _tuned(op, x).forward(x)
 
 
 def _bwd(op, x):
-    return op.backward(x)
+    return _tuned(op, x).backward(x)
 
 
 def _smooth_at_least(n):

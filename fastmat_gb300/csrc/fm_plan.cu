@@ -388,10 +388,11 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   auto lsmem = [&](int B, int Lp, int nb) {
     return fmk::launch_smem(B, Lp, esz, nb) + extra;
   };
+  // the deepest ring (4 .. 2 buffers) that still lets two CTAs share an SM
   auto pick_nbuf = [&](int B, int Lp) {
     if (want_nbuf) return want_nbuf;
     int nb = 4;
-    while (nb > 2 && lsmem(B, Lp, nb) > (size_t)150 * 1024)
+    while (nb > 2 && lsmem(B, Lp, nb) > (size_t)112 * 1024)
       --nb;
     return nb;
   };

@@ -14,6 +14,7 @@ import threading
 from . import _native
 
 _lock = threading.Lock()
+_mem = {}   # key -> entry, the choices this process has applied already
 
 
 def cache_path():
@@ -61,12 +62,20 @@ def autotune(plan, num_cols, cache=True):
     import torch
     key = _key(plan, num_cols)
     with _lock:
+        if cache and key in _mem:
+            if getattr(plan, '_tuned_key', None) != key:
+                for d in (_native.FORWARD, _native.BACKWARD):
+                    plan.set_tiles(d, _mem[key][str(d)])
+                plan._tuned_key = key
+            return _mem[key]
         db = _load() if cache else {}
         entry = db.get(key)
         if entry is not None:
             try:
                 for d in (_native.FORWARD, _native.BACKWARD):
                     plan.set_tiles(d, entry[str(d)])
+                _mem[key] = entry
+                plan._tuned_key = key
                 return entry
             except (ValueError, KeyError):
                 pass
@@ -79,4 +88,6 @@ def autotune(plan, num_cols, cache=True):
             db = _load()
             db[key] = entry
             _store(db)
+            _mem[key] = entry
+            plan._tuned_key = key
         return entry
