@@ -2983,8 +2983,19 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: sparse operators run "
                                    "outside batches");
         // (register convolutions and FWHTs run as their vector program)
-        LStep ls = ls0;  // register convolutions run as their vector program
-        if (!configure(esz, ls, 0, 0, false, 0, false))
+        LStep ls = ls0;
+        // vectors per tile: as many as keep the batch's 512-thread CTA busy
+        // (up to one work item per thread) within a 48 KB tile slot
+        int wantB = 0;
+        for (int b = 1; b <= 1024; b *= 2) {
+          LStep t = ls0;
+          if (!configure(esz, t, b, 2, false, 0, false)) continue;
+          if (t.threads > FM_MAX_THREADS ||
+              fmk::tile_bytes(b, t.st.Lp, esz) > (size_t)48 * 1024)
+            break;
+          wantB = b;
+        }
+        if (!configure(esz, ls, wantB, 0, false, 0, false))
           fail(FM_ERR_UNSUPPORTED, "fm_batch_create: a launch has no "
                                    "vector-major tile shape");
         fmk::Step st = ls.st;
