@@ -2905,6 +2905,49 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
   });
 }
 
+// The register tile program (fm_rtile.cuh) a complex64 batch step runs, or
+// 0 when its vector program is not one of the shapes it covers:
+// [zero pad] DIF(L) [twiddle] or [zero pad] DIF(L) product DIT(L) [twiddle],
+// L = 64 .. 512 with the radix sequence (8, 8, ..., rest).
+static int rtile_shape(const fmk::Step &st) {
+  const int L = st.L;
+  if (L != 64 && L != 128 && L != 256 && L != 512) return 0;
+  if (st.out_mode == 1 || st.nops < 1) return 0;
+  auto radices_ok = [&](const fmk::Op &op) {
+    if (op.len != L || op.nrad != fmk::rc_stages(L, fmk::kRtP)) return false;
+    for (int i = 0; i < op.nrad; ++i)
+      if (op.rad[i] != fmk::rc_radix(i, L, fmk::kRtP)) return false;
+    return true;
+  };
+  int f = 0, o = 0, end = st.nops;
+  if (st.ops[0].kind == fmk::OP_ZPAD) {
+    if (st.ops[0].len2 != L || st.ops[0].len > L) return 0;
+    f |= fmk::RT_ZPAD;
+    o = 1;
+  }
+  if (end > o + 1 && st.ops[end - 1].kind == fmk::OP_TW) {
+    const fmk::Op &t = st.ops[end - 1];
+    if (t.len != L || t.N <= 0 || t.div < 1 || t.mod < 1) return 0;
+    f |= fmk::RT_TW;
+    --end;
+  }
+  if (o >= end) return 0;
+  const fmk::Op &d = st.ops[o];
+  if (d.kind != fmk::OP_DIF || !radices_ok(d)) return 0;
+  if (end == o + 1) {
+    if ((f & fmk::RT_TW) && !st.ops[st.nops - 1].ptr2) return 0;
+    return f | fmk::RT_FFT | (d.sign > 0 ? fmk::RT_INV : 0);
+  }
+  if (end == o + 3 && st.ops[o + 1].kind == fmk::OP_MUL &&
+      st.ops[o + 1].len == L && st.ops[o + 1].div >= 1 &&
+      st.ops[o + 1].mod >= 1 && st.ops[o + 2].kind == fmk::OP_DIT &&
+      radices_ok(st.ops[o + 2]) && d.sign < 0 && st.ops[o + 2].sign > 0) {
+    if ((f & fmk::RT_TW) && st.ops[st.nops - 1].ptr2) return 0;
+    return f | fmk::RT_CONV;
+  }
+  return 0;
+}
+
 int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
                     const int32_t *directions, const void *const *x,
                     const int32_t *x_types, const int64_t *ld_x,
@@ -3023,6 +3066,7 @@ int fm_batch_create(int32_t num_ops, fm_plan *const *plans,
         st.num_cols = M;
         st.err = B->status + 1;
         st.tma_in = st.tma_out = 0;
+        st.rprog = ctype == FM_C64 ? rtile_shape(st) : 0;
         const i64 tiles = (st.V * M + st.B - 1) / st.B;
         if (st.V * M >= 0x7fffffffLL)
           fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");

@@ -64,22 +64,10 @@ struct RcStep {
 };
 
 // ---- compile-time plan: P points per lane, radices (P, P, ..., rest)
+// (rc_stages / rc_radix / rc_mprev / rc_log2 in fm_rtile.cuh)
 template <class E> struct RcLane {
   static constexpr int P = sizeof(E) == 8 ? 16 : 8;
 };
-__host__ __device__ constexpr int rc_stages(int L, int P) {
-  return L <= P ? 1 : 1 + rc_stages(L / P, P);
-}
-__host__ __device__ constexpr int rc_radix(int i, int L, int P) {
-  return i == 0 ? (L < P ? L : P) : rc_radix(i - 1, L / P, P);
-}
-// L / (R_0 ... R_{i-1})
-__host__ __device__ constexpr int rc_mprev(int i, int L, int P) {
-  return i == 0 ? L : rc_mprev(i - 1, L, P) / rc_radix(i - 1, L, P);
-}
-__host__ __device__ constexpr int rc_log2(int n) {
-  return n <= 1 ? 0 : 1 + rc_log2(n / 2);
-}
 
 // Shared-memory layout of a vector's exchange buffer: point p at
 // p + (p >> SH), vectors Lp points apart; its input slot: natural order,
@@ -177,7 +165,8 @@ __device__ __forceinline__ int rc_base(int g) {
   constexpr int P = RcLane<E>::P;
   constexpr int Mprev = rc_mprev(I, L, P);
   constexpr int M = Mprev / rc_radix(I, L, P);
-  return (g >> rc_log2(M)) * Mprev + (g & (M - 1));
+  constexpr int LM = rc_log2(M);
+  return (g >> LM) * Mprev + (g & (M - 1));
 }
 template <class E, int L, int I>
 __device__ __forceinline__ int rc_off(int j) {  // register j = u R + r

@@ -1,0 +1,307 @@
+// Register-resident FFT programs on vector-major tiles (complex64), for the
+// batched kernel: the passes of long transforms (fastmat/Fourier.pyx and the
+// convolutions of fastmat/Circulant.pyx:127-133 split four-step as
+// N = N1 N2) and short convolutions, whose vector programs are
+//
+//   RT_FFT:   [zero pad] DIF(L) [twiddle] -> natural order
+//   RT_CONV:  [zero pad] DIF(L) spectrum product DIT(L) [twiddle]
+//
+// for power-of-two L = 64 .. 512 with the planner's radix sequence
+// (8, 8, ..., rest).  The generic tile program runs each FFT stage and each
+// product as a pass over the shared-memory tile with run-time index
+// arithmetic; here a vector's L points sit in the registers of G = L / 8
+// threads (8 points each, natural order g + G r after the load), the
+// radix-8 / 4 / 2 stages run in registers with compile-time positions and
+// exchange through the vector's own storage in the tile, the twiddle and
+// spectrum products are applied on the registers, and the results go back
+// to the tile in natural order (the storer's digit-reversal table is then
+// not used).  The arithmetic is the generic program's, operation for
+// operation (same stage order, twiddle tables and products), so the results
+// are bit-identical to it.
+//
+// Positions follow the in-place DIF of the generic program: stage i with
+// radix R, Mprev = L / (R_0 ... R_{i-1}) and M = Mprev / R takes, for block K
+// and t < M, the points K Mprev + t + M r.  Thread g's butterflies at stage
+// i are w = g + G u (u < 8 / R); M divides G, so t = g mod M and the position
+// is a per-thread base plus a compile-time offset u G R + M r.
+#pragma once
+
+namespace fmk {
+
+// ---- compile-time radix plan: P points per thread, radices (P, ..., rest)
+__host__ __device__ constexpr int rc_stages(int L, int P) {
+  return L <= P ? 1 : 1 + rc_stages(L / P, P);
+}
+__host__ __device__ constexpr int rc_radix(int i, int L, int P) {
+  return i == 0 ? (L < P ? L : P) : rc_radix(i - 1, L / P, P);
+}
+// L / (R_0 ... R_{i-1})
+__host__ __device__ constexpr int rc_mprev(int i, int L, int P) {
+  return i == 0 ? L : rc_mprev(i - 1, L, P) / rc_radix(i - 1, L, P);
+}
+__host__ __device__ constexpr int rc_log2(int n) {
+  return n <= 1 ? 0 : 1 + rc_log2(n / 2);
+}
+
+// Step::rprog: program shape (bits 0-1) and flags
+enum {
+  RT_NONE = 0,
+  RT_FFT = 1,
+  RT_CONV = 2,
+  RT_ZPAD = 4,  // ops[0] is a zero pad
+  RT_TW = 8,    // the last op is a twiddle product
+  RT_INV = 16   // RT_FFT: the transform has sign +1
+};
+constexpr int kRtP = 8;  // points per thread
+
+template <int L, int I>
+__device__ __forceinline__ int rt_base(int g) {
+  constexpr int Mprev = rc_mprev(I, L, kRtP);
+  constexpr int M = Mprev / rc_radix(I, L, kRtP);
+  constexpr int LM = rc_log2(M);
+  return (g >> LM) * Mprev + (g & (M - 1));
+}
+template <int L, int I>
+__host__ __device__ constexpr int rt_off(int j) {  // register j = u R + r
+  constexpr int R = rc_radix(I, L, kRtP);
+  constexpr int M = rc_mprev(I, L, kRtP) / R;
+  return (j / R) * (L / kRtP) * R + M * (j % R);
+}
+// natural index of DIF output position p: the position's digits (radix
+// R_0 most significant) read in reverse
+template <int L, int I>
+__host__ __device__ constexpr int rt_below() {  // bits of the digits > I
+  if constexpr (I + 1 >= rc_stages(L, kRtP))
+    return 0;
+  else
+    return rc_log2(rc_radix(I + 1, L, kRtP)) + rt_below<L, I + 1>();
+}
+template <int L, int I>
+__device__ __forceinline__ int rt_nat_from(int p, int sh) {
+  constexpr int S = rc_stages(L, kRtP);
+  if constexpr (I >= S) {
+    return 0;
+  } else {
+    constexpr int BI = rc_log2(rc_radix(I, L, kRtP));
+    constexpr int BELOW = rt_below<L, I>();
+    return (((p >> BELOW) & ((1 << BI) - 1)) << sh) |
+           rt_nat_from<L, I + 1>(p, sh + BI);
+  }
+}
+template <int L>
+__device__ __forceinline__ int rt_nat(int p) {
+  return rt_nat_from<L, 0>(p, 0);
+}
+
+template <int L>
+__device__ __forceinline__ void rt_sync() {
+  if constexpr (L / kRtP > 32)
+    __syncthreads();  // a vector spans several warps
+  else
+    __syncwarp();
+}
+
+// stage I: DIF (DFT, then twiddles of the outputs) or DIT (twiddles of the
+// inputs, then DFT), transform sign SG; register u R + r holds position
+// base + u G R + M r before and after
+template <int L, int I, bool DIT, int SG>
+__device__ __forceinline__ void rt_stage(float2 (&x)[kRtP], int g,
+                                         const float2 *__restrict__ tw) {
+  constexpr int R = rc_radix(I, L, kRtP);
+  constexpr int Mprev = rc_mprev(I, L, kRtP);
+  constexpr int M = Mprev / R;
+  constexpr int NB = kRtP / R;
+  constexpr int TS = L / Mprev;  // table stride of w_Mprev in tw (length L)
+  float2 w[R];
+  if constexpr (M > 1) {
+    const int t = g & (M - 1);
+#pragma unroll
+    for (int k = 1; k < R; ++k) w[k] = __ldg(tw + t * k * TS);
+  }
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = x[u * R + r];
+    if constexpr (DIT && M > 1) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul_lazy<SG>(v[k], w[k]);
+    }
+    dif_stages<R, R / 2>(v, SG);  // v[i] = output brev(i)
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      float2 y = v[i];
+      const int k = brev<R>(i);
+      if constexpr (!DIT && M > 1) {
+        if (k != 0) y = cmul_lazy<SG>(y, w[k]);
+      }
+      x[u * R + k] = y;
+    }
+  }
+}
+
+// registers laid out for stage IA -> the vector's tile storage ->
+// registers laid out for stage IB
+template <int L, int IA, int IB>
+__device__ __forceinline__ void rt_exchange(float2 (&x)[kRtP], float2 *vec,
+                                            int g, bool act) {
+  const int ba = rt_base<L, IA>(g), bb = rt_base<L, IB>(g);
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < kRtP; ++j)
+      vec[pidx<float2>(ba + rt_off<L, IA>(j))] = x[j];
+  }
+  rt_sync<L>();
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < kRtP; ++j)
+      x[j] = vec[pidx<float2>(bb + rt_off<L, IB>(j))];
+  }
+  rt_sync<L>();
+}
+
+template <int L, int I, int SG>
+__device__ __forceinline__ void rt_forward(float2 (&x)[kRtP], float2 *vec,
+                                           int g, bool act,
+                                           const float2 *tw) {
+  rt_stage<L, I, false, SG>(x, g, tw);
+  constexpr int S = rc_stages(L, kRtP);
+  if constexpr (I + 1 < S) {
+    rt_exchange<L, I, I + 1>(x, vec, g, act);
+    rt_forward<L, I + 1, SG>(x, vec, g, act, tw);
+  }
+}
+template <int L, int I, int SG>
+__device__ __forceinline__ void rt_inverse(float2 (&x)[kRtP], float2 *vec,
+                                           int g, bool act,
+                                           const float2 *tw) {
+  rt_stage<L, I, true, SG>(x, g, tw);
+  if constexpr (I > 0) {
+    rt_exchange<L, I, I - 1>(x, vec, g, act);
+    rt_inverse<L, I - 1, SG>(x, vec, g, act, tw);
+  }
+}
+
+// twiddle product of the generic program (OP_TW): e *= w_N^(+-q nat),
+// the op's fields held in registers
+struct RtTw {
+  const float2 *tab;
+  i64 N;
+  bool neg;
+  unsigned q;
+  __device__ __forceinline__ float2 apply(float2 e, int nat) const {
+    i64 t = (i64)q * nat;
+    if (t >= N) t %= N;
+    const float2 wv = __ldg(tab + t);
+    return neg ? cmul(e, wv) : cmulc(e, wv);
+  }
+};
+__device__ __forceinline__ RtTw rt_tw(const Op &op, unsigned vcol) {
+  RtTw t;
+  t.tab = (const float2 *)op.ptr;
+  t.N = op.N;
+  t.neg = op.sign < 0;
+  t.q = (op.div == 1 && op.mod == 1)
+            ? 0u
+            : (vcol / (unsigned)op.div) % (unsigned)op.mod;
+  return t;
+}
+
+// The whole tile program of a step with rprog != 0 on the B vectors of a
+// vector-major tile; leaves the results in natural order.  All threads of
+// the CTA take part (barriers for L = 512).
+template <int L, int SHAPE, int SG>
+__device__ __noinline__ void rt_program_l(const Step &p, float2 *sm,
+                                          const VInfo *vi, int tid, int T) {
+  constexpr int G = L / kRtP;
+  constexpr int S = rc_stages(L, kRtP);
+  // (the launch record lives in shared memory like the tile: the fields a
+  // loop over points uses are read into registers first, each where it is
+  // needed, to keep the registers of the transforms free)
+  const int B = p.B, Lp = p.Lp;
+  const int nvr = T / G;
+  const int f = p.rprog;
+  const int o0 = (f & RT_ZPAD) ? 1 : 0;
+  const int zfrom = o0 ? p.ops[0].len : L;
+  const bool has_tw = (f & RT_TW) != 0;
+  for (int b0 = 0; b0 < B; b0 += nvr) {
+    const int b = b0 + tid / G, g = tid % G;
+    const bool act = b < B;
+    float2 *vec = sm + (act ? b : 0) * Lp;
+    const unsigned vcol = act ? (unsigned)vi[b].vcol : 0u;
+    const float2 *const twf = (const float2 *)p.ops[o0].ptr;
+    float2 x[kRtP];
+#pragma unroll
+    for (int r = 0; r < kRtP; ++r) {
+      const int j = g + G * r;
+      x[r] = (act && j < zfrom) ? vec[pidx<float2>(j)] : make_float2(0.f, 0.f);
+    }
+    // (stage 0 writes each thread's exchange values to the positions it has
+    // just read, so no barrier is needed before the first exchange)
+    if constexpr (SHAPE == RT_CONV) {
+      rt_forward<L, 0, -1>(x, vec, g, act, twf);
+      {
+        const Op &mul = p.ops[o0 + 1];
+        const unsigned mdiv = (unsigned)mul.div, mmod = (unsigned)mul.mod;
+        const unsigned q =
+            (mdiv == 1 && mmod == 1) ? 0u : (vcol / mdiv) % mmod;
+        const float2 *P = (const float2 *)mul.ptr + (int)q * (int)mul.stride;
+        const bool mconj = mul.sign != 0;
+        const int bl = rt_base<L, S - 1>(g);
+#pragma unroll
+        for (int j = 0; j < kRtP; ++j)
+          x[j] = mulv(x[j], __ldg(P + bl + rt_off<L, S - 1>(j)), mconj);
+      }
+      rt_inverse<L, S - 1, +1>(x, vec, g, act,
+                               (const float2 *)p.ops[o0 + 2].ptr);
+      // natural order: register r holds point g + G r
+      if (has_tw) {
+        const RtTw tw = rt_tw(p.ops[p.nops - 1], vcol);
+#pragma unroll
+        for (int r = 0; r < kRtP; ++r) x[r] = tw.apply(x[r], g + G * r);
+      }
+      if (act) {
+#pragma unroll
+        for (int r = 0; r < kRtP; ++r) vec[pidx<float2>(g + G * r)] = x[r];
+      }
+    } else {
+      rt_forward<L, 0, SG>(x, vec, g, act, twf);
+      const int bl = rt_base<L, S - 1>(g);
+      RtTw tw;
+      if (has_tw) tw = rt_tw(p.ops[p.nops - 1], vcol);
+#pragma unroll
+      for (int j = 0; j < kRtP; ++j) {
+        const int nat = rt_nat<L>(bl + rt_off<L, S - 1>(j));
+        float2 y = x[j];
+        if (has_tw) y = tw.apply(y, nat);
+        if (act) vec[pidx<float2>(nat)] = y;
+      }
+    }
+    rt_sync<L>();
+  }
+  __syncthreads();
+}
+
+template <int SHAPE, int SG>
+__device__ __forceinline__ void rt_program_s(const Step &p, float2 *sm,
+                                             const VInfo *vi, int tid,
+                                             int T) {
+  switch (p.L) {
+    case 64: rt_program_l<64, SHAPE, SG>(p, sm, vi, tid, T); break;
+    case 128: rt_program_l<128, SHAPE, SG>(p, sm, vi, tid, T); break;
+    case 256: rt_program_l<256, SHAPE, SG>(p, sm, vi, tid, T); break;
+    default: rt_program_l<512, SHAPE, SG>(p, sm, vi, tid, T); break;
+  }
+}
+
+__device__ __forceinline__ void rt_program(const Step &p, float2 *sm,
+                                           const VInfo *vi, int tid, int T) {
+  if ((p.rprog & 3) == RT_CONV)
+    rt_program_s<RT_CONV, -1>(p, sm, vi, tid, T);
+  else if (p.rprog & RT_INV)
+    rt_program_s<RT_FFT, +1>(p, sm, vi, tid, T);
+  else
+    rt_program_s<RT_FFT, -1>(p, sm, vi, tid, T);
+}
+
+}  // namespace fmk

@@ -88,7 +88,7 @@ struct Step {
   i64 num_cols;
   long long wait_limit;  // polls of a bounded copy wait before it gives up
   int nops;
-  int pad_;
+  int rprog;  // register tile program of the batched kernel (RT_*)
   Op ops[FM_MAX_OPS];
 };
 
@@ -1244,10 +1244,14 @@ __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
 template <class E, int LAY>
 __device__ __forceinline__ void load_async(const Step &p, E *sm,
                                            const VInfo *vi, int tid, int T) {
+  // (the launch record may sit in shared memory: its fields are read once,
+  // so the copies below need not reload them)
   const int B = p.B, L = p.L, Lp = p.Lp;
   const int total = B * L;
   const E *src = (const E *)p.src;
   const i64 cc = p.vin.Cc;
+  const int in_len = p.in_len;
+  const i64 in_rows = p.in_rows;
   const int lgB = __ffs(B) - 1;
   Walk w(tid, L, T);
   for (int f = tid; f < total; f += T, w.next()) {
@@ -1261,7 +1265,7 @@ __device__ __forceinline__ void load_async(const Step &p, E *sm,
     }
     const i64 rb = vi[b].rb_in;
     const i64 r = rb + (i64)j * cc;
-    const bool ok = rb >= 0 && j < p.in_len && r < p.in_rows;
+    const bool ok = rb >= 0 && j < in_len && r < in_rows;
     cp_async<sizeof(E)>(vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B),
                         ok ? (const void *)(src + vi[b].col_src + r)
                            : (const void *)src,
@@ -1314,6 +1318,10 @@ __device__ __forceinline__ void load_fixup(const Step &p, E *sm,
   const int B = p.B, L = p.L, Lp = p.Lp;
   const int total = B * L;
   const i64 cc = p.vin.Cc;
+  const int in_len = p.in_len;
+  const i64 in_rows = p.in_rows;
+  const bool conj_in = p.conj_in != 0;
+  const E *const pre = (const E *)p.pre;
   const int lgB = __ffs(B) - 1;
   Walk w(tid, L, T);
   for (int f = tid; f < total; f += T, w.next()) {
@@ -1326,13 +1334,13 @@ __device__ __forceinline__ void load_fixup(const Step &p, E *sm,
       j = w.j;
     }
     const i64 rb = vi[b].rb_in;
-    if (rb < 0 || j >= p.in_len) continue;
+    if (rb < 0 || j >= in_len) continue;
     const i64 r = rb + (i64)j * cc;
-    if (r >= p.in_rows) continue;
+    if (r >= in_rows) continue;
     E *e = vbase<E, LAY>(sm, b, Lp) + jx<E, LAY>(j, B);
     E val = *e;
-    if (p.conj_in) val = conjv(val);
-    if (p.pre) val = mulv(val, ((const E *)p.pre)[r], false);
+    if (conj_in) val = conjv(val);
+    if (pre) val = mulv(val, pre[r], false);
     *e = val;
   }
 }
@@ -1384,7 +1392,8 @@ __device__ __forceinline__ void store_fixup_em(const Step &p, E *sm,
 template <class E, int LAY>
 __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
                                            const VInfo *vi, const int *sexp,
-                                           int tid, int T) {
+                                           int tid, int T,
+                                           bool natural = false) {
   const int B = p.B, Lp = p.Lp;
   const bool acc = p.accumulate != 0;
   const E c = scalar_of<E>(p.scale_re, p.scale_im);
@@ -1406,10 +1415,22 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
       return;
     }
   }
+  // (the launch record may sit in shared memory, and the compiler cannot
+  // rule out that the global stores below alias it: its fields are read
+  // into registers once)
   const i64 ccout = p.vout.Cc;
-  const int total = B * p.out_len;
+  const int out_len = p.out_len;
+  const int total = B * out_len;
   const int lgB = __ffs(B) - 1;
-  Walk w(tid, p.out_len, T);
+  const i64 out_rows = p.out_rows;
+  const i64 *const map_out = p.out_mode == 2 ? p.map_out : nullptr;
+  const int *const out_pos = natural ? nullptr : p.out_pos;
+  const E *const post = (const E *)p.post;
+  const bool has_scale = p.has_scale != 0, conj_out = p.conj_out != 0;
+  const bool raw = p.dst_type == Tr<E>::code && !acc;
+  void *const dst = p.dst;
+  const int dst_type = p.dst_type;
+  Walk w(tid, out_len, T);
   for (int f = tid; f < total; f += T, w.next()) {
     int b, j;
     if (ccout > 1 || LAY == 1) {
@@ -1422,25 +1443,24 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
     const i64 rb = vi[b].rb_out;
     if (rb < 0) continue;
     const i64 r = rb + (i64)j * ccout;
-    if (r >= p.out_rows) continue;
-    const i64 drow = p.out_mode == 2 ? p.map_out[r] : r;
+    if (r >= out_rows) continue;
+    const i64 drow = map_out ? map_out[r] : r;
     if (drow < 0) continue;
     E val = vbase<E, LAY>(const_cast<E *>(sm), b, Lp)
-        [jx<E, LAY>(p.out_pos ? p.out_pos[j] : j, B)];
-    if (p.post) val = mulv(val, ((const E *)p.post)[r], false);
-    if (p.has_scale) val = mulv(val, c, false);
-    if (p.conj_out) val = conjv(val);
+        [jx<E, LAY>(out_pos ? out_pos[j] : j, B)];
+    if (post) val = mulv(val, post[r], false);
+    if (has_scale) val = mulv(val, c, false);
+    if (conj_out) val = conjv(val);
     if constexpr (Emu<E>::v) {
-      if (p.dst_type == Tr<E>::code && !acc)
-        ((E *)p.dst)[vi[b].col_dst + drow] = to_bits(val, sexp[b]);
+      if (raw)
+        ((E *)dst)[vi[b].col_dst + drow] = to_bits(val, sexp[b]);
       else
-        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc,
-                    sexp[b]);
+        store_as<E>(dst, dst_type, vi[b].col_dst + drow, val, acc, sexp[b]);
     } else {
-      if (p.dst_type == Tr<E>::code && !acc)
-        ((E *)p.dst)[vi[b].col_dst + drow] = val;
+      if (raw)
+        ((E *)dst)[vi[b].col_dst + drow] = val;
       else
-        store_as<E>(p.dst, p.dst_type, vi[b].col_dst + drow, val, acc);
+        store_as<E>(dst, dst_type, vi[b].col_dst + drow, val, acc);
     }
   }
 }
@@ -1835,6 +1855,10 @@ __host__ __device__ __forceinline__ size_t batch_smem(int max_B,
   return batch_head_bytes(max_B) + 2 * max_tile;
 }
 
+}  // namespace fmk
+#include "fm_rtile.cuh"
+namespace fmk {
+
 // Loads of one batch tile into a slot: cp.async when the source already
 // has the compute type and needs no gather (completion is awaited later,
 // so the copy overlaps the previous tile's program), synchronous loads with
@@ -1932,7 +1956,16 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
         __syncthreads();
       }
       const int nwarps = T >> 5;
-      if (warp_mode<E, CLS, 0>(p.B, p.L, nwarps)) {
+      bool natural = false;
+      if constexpr (std::is_same<E, float2>::value) {
+        if (p.rprog) {
+          // the program on registers; results in natural order
+          rt_program(p, sm, vi, tid, T);
+          natural = true;
+        }
+      }
+      if (natural) {
+      } else if (warp_mode<E, CLS, 0>(p.B, p.L, nwarps)) {
         const int w = tid >> 5, vw = p.B / nwarps;
         run_program<E, CLS, 0>(p, sm + w * vw * p.Lp, p.Lp, vw, vi + w * vw,
                                sq + w * vw, tid & 31, 32);
@@ -1940,7 +1973,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       } else {
         run_program<E, CLS, 0>(p, sm, p.Lp, p.B, vi, sq, tid, T);
       }
-      store_tile<E, 0>(p, sm, vi, sexp, tid, T);
+      store_tile<E, 0>(p, sm, vi, sexp, tid, T, natural);
       __syncthreads();
       cur ^= 1;
       kc = kn;
