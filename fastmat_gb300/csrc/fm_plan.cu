@@ -184,6 +184,22 @@ __global__ void k_twiddle(E *tw, i64 N) {
   }
 }
 
+// Two-level twiddle table of length-N transforms: w^e = T1[e >> s] T0[e & (2^s - 1)],
+// T0[j] = w^j (j < 2^s) at tw[j], T1[m] = w^(m 2^s) (m <= (N - 1) >> s) at
+// tw[2^s + m], w = exp(-2 pi i / N); both factors small enough to stay in
+// the L1 cache.
+template <class E>
+__global__ void k_twiddle2(E *tw, i64 N, int s) {
+  const i64 n0 = 1LL << s, n1 = ((N - 1) >> s) + 1;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n0 + n1;
+       t += (i64)gridDim.x * blockDim.x) {
+    const i64 e = t < n0 ? t : (t - n0) << s;
+    double sn, c;
+    sincospi(-2.0 * (double)e / (double)N, &sn, &c);
+    tw[t] = mk<E>(c, sn);
+  }
+}
+
 // Bluestein chirp a[n] = exp(-i pi n^2 / N) with n^2 reduced mod 2N exactly
 __global__ void k_chirp(double2 *a, i64 N) {
   for (i64 n = blockIdx.x * (i64)blockDim.x + threadIdx.x; n < N;
@@ -554,6 +570,25 @@ class Planner {
       k_twiddle<double2><<<grid_for(N), 256>>>((double2 *)p, N);
     CUDA_TRY(cudaGetLastError());
     P_->twiddles[N] = p;
+    return p;
+  }
+
+  // split of the two-level twiddle table of length N (complex64 only)
+  static int twiddle2_bits(i64 N) {
+    int b = 0;
+    while ((1LL << b) < N) ++b;
+    return (b + 1) / 2;
+  }
+  const void *twiddle2(i64 N) {
+    if (P_->ctype != FM_C64) return nullptr;
+    auto it = P_->twiddles.find(-N);
+    if (it != P_->twiddles.end()) return it->second;
+    const int s = twiddle2_bits(N);
+    const i64 n = (1LL << s) + ((N - 1) >> s) + 1;
+    void *p = dalloc((size_t)n * P_->esz);
+    k_twiddle2<float2><<<grid_for(n), 256>>>((float2 *)p, N, s);
+    CUDA_TRY(cudaGetLastError());
+    P_->twiddles[-N] = p;
     return p;
   }
 
@@ -958,6 +993,7 @@ class Planner {
     a.ops.push_back(fft_op(L1, -1));
     fmk::Op tw = mkop(fmk::OP_TW, (int)L1);
     tw.ptr = twiddle(L);
+    tw.ptr3 = twiddle2(L);
     tw.N = L;
     tw.sign = -1;
     tw.div = 1;
@@ -978,6 +1014,7 @@ class Planner {
     b.ops.push_back(fft_op(L2, +1));
     fmk::Op tw2 = mkop(fmk::OP_TW, (int)L2);
     tw2.ptr = twiddle(L);
+    tw2.ptr3 = twiddle2(L);
     tw2.N = L;
     tw2.sign = +1;
     tw2.div = 1;
@@ -1024,6 +1061,7 @@ class Planner {
       a.ops.push_back(fft_op(N1, sign));
       fmk::Op tw = mkop(fmk::OP_TW, (int)N1);
       tw.ptr = twiddle(N);
+      tw.ptr3 = twiddle2(N);
       tw.N = N;
       tw.sign = sign;
       tw.div = 1;
@@ -2927,7 +2965,8 @@ static int rtile_shape(const fmk::Step &st) {
   }
   if (end > o + 1 && st.ops[end - 1].kind == fmk::OP_TW) {
     const fmk::Op &t = st.ops[end - 1];
-    if (t.len != L || t.N <= 0 || t.div < 1 || t.mod < 1) return 0;
+    if (t.len != L || t.N <= 0 || t.div < 1 || t.mod < 1 || !t.ptr3)
+      return 0;
     f |= fmk::RT_TW;
     --end;
   }

@@ -16,8 +16,9 @@
 // spectrum products are applied on the registers, and the results go back
 // to the tile in natural order (the storer's digit-reversal table is then
 // not used).  The arithmetic is the generic program's, operation for
-// operation (same stage order, twiddle tables and products), so the results
-// are bit-identical to it.
+// operation (same stage order, twiddle tables and products) except for the
+// four-step twiddle product, which takes its factor from a two-level table
+// (one more rounding; see RtTw).
 //
 // Positions follow the in-place DIF of the generic program: stage i with
 // radix R, Mprev = L / (R_0 ... R_{i-1}) and M = Mprev / R takes, for block K
@@ -182,24 +183,35 @@ __device__ __forceinline__ void rt_inverse(float2 (&x)[kRtP], float2 *vec,
   }
 }
 
-// twiddle product of the generic program (OP_TW): e *= w_N^(+-q nat),
-// the op's fields held in registers
+// twiddle product (OP_TW): e *= w_N^(+-q nat), w = exp(-2 pi i / N), from
+// the op's two-level table (ptr3: w^e = T1[e >> s] T0[e & (2^s - 1)],
+// s = ceil(log2(N) / 2)), whose two factors stay in the L1 cache where the
+// N-entry table of the generic program is read from L2 at random; one more
+// rounding than the full table
 struct RtTw {
-  const float2 *tab;
+  const float2 *t0, *t1;
   i64 N;
+  int s;
   bool neg;
   unsigned q;
   __device__ __forceinline__ float2 apply(float2 e, int nat) const {
     i64 t = (i64)q * nat;
     if (t >= N) t %= N;
-    const float2 wv = __ldg(tab + t);
+    const float2 a = __ldg(t1 + (t >> s));
+    const float2 b = __ldg(t0 + (t & ((1 << s) - 1)));
+    const float2 wv = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
     return neg ? cmul(e, wv) : cmulc(e, wv);
   }
 };
 __device__ __forceinline__ RtTw rt_tw(const Op &op, unsigned vcol) {
   RtTw t;
-  t.tab = (const float2 *)op.ptr;
-  t.N = op.N;
+  const i64 N = op.N;
+  int b = 0;
+  while ((1LL << b) < N) ++b;
+  t.s = (b + 1) / 2;
+  t.t0 = (const float2 *)op.ptr3;
+  t.t1 = t.t0 + (1 << t.s);
+  t.N = N;
   t.neg = op.sign < 0;
   t.q = (op.div == 1 && op.mod == 1)
             ? 0u

@@ -47,6 +47,8 @@ struct Op {
   unsigned char rad[16];  // FFT radices / FWHT bit-group widths
   const void *ptr;        // twiddles, vector, map, matrix
   const int *ptr2;        // TW: storage position -> natural index
+  const void *ptr3;       // TW (complex64): two-level table, see
+                          // twiddle2 in the planner
   i64 div, mod, stride;   // q = (v / div) % mod for MUL / TW
   i64 N;
   double sre, sim;
