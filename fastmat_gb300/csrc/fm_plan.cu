@@ -2982,7 +2982,11 @@ static int rtile_shape(const fmk::Step &st) {
       st.ops[o + 1].mod >= 1 && st.ops[o + 2].kind == fmk::OP_DIT &&
       radices_ok(st.ops[o + 2]) && d.sign < 0 && st.ops[o + 2].sign > 0) {
     if ((f & fmk::RT_TW) && st.ops[st.nops - 1].ptr2) return 0;
-    return f | fmk::RT_CONV;
+    f |= fmk::RT_CONV;
+    if (st.vout.Cc == 1 && st.out_mode == 0 && st.dst_type == FM_C64 &&
+        !st.accumulate)
+      f |= fmk::RT_DIRECT;
+    return f;
   }
   return 0;
 }

@@ -51,7 +51,9 @@ enum {
   RT_CONV = 2,
   RT_ZPAD = 4,  // ops[0] is a zero pad
   RT_TW = 8,    // the last op is a twiddle product
-  RT_INV = 16   // RT_FFT: the transform has sign +1
+  RT_INV = 16,  // RT_FFT: the transform has sign +1
+  RT_DIRECT = 32  // RT_CONV: results stored from registers (contiguous
+                  // complex64 output, plain store): no storer pass
 };
 constexpr int kRtP = 8;  // points per thread
 
@@ -272,7 +274,30 @@ __device__ __noinline__ void rt_program_l(const Step &p, float2 *sm,
 #pragma unroll
         for (int r = 0; r < kRtP; ++r) x[r] = tw.apply(x[r], g + G * r);
       }
-      if (act) {
+      if (f & RT_DIRECT) {
+        // consecutive threads hold consecutive points: coalesced stores;
+        // post-product, scale and conjugation in the storer's order
+        const i64 rb = act ? vi[b].rb_out : -1;
+        if (rb >= 0) {
+          float2 *dst = (float2 *)p.dst + vi[b].col_dst + rb;
+          const int out_len = p.out_len;
+          const i64 lim = p.out_rows - rb;
+          const float2 *post = (const float2 *)p.post;
+          const bool has_scale = p.has_scale != 0, conj_out = p.conj_out != 0;
+          const float2 c = scalar_of<float2>(p.scale_re, p.scale_im);
+#pragma unroll
+          for (int r = 0; r < kRtP; ++r) {
+            const int j = g + G * r;
+            if (j < out_len && j < lim) {
+              float2 val = x[r];
+              if (post) val = mulv(val, post[rb + j], false);
+              if (has_scale) val = mulv(val, c, false);
+              if (conj_out) val = conjv(val);
+              dst[j] = val;
+            }
+          }
+        }
+      } else if (act) {
 #pragma unroll
         for (int r = 0; r < kRtP; ++r) vec[pidx<float2>(g + G * r)] = x[r];
       }

@@ -1255,6 +1255,32 @@ __device__ __forceinline__ void load_async(const Step &p, E *sm,
   const int in_len = p.in_len;
   const i64 in_rows = p.in_rows;
   const int lgB = __ffs(B) - 1;
+  if constexpr (LAY == 0 && sizeof(E) == 8) {
+    if (cc == 1 && (Lp & 1) == 0 && (L & (L - 1)) == 0 &&
+        ((size_t)src & 15) == 0) {
+      // contiguous vectors of a power-of-two length: pairs of points as one
+      // 16-byte copy where both exist and the source pair is aligned
+      const int lgh = __ffs(L) - 2;  // log2(L / 2)
+      for (int f = tid; f < total / 2; f += T) {
+        const int b = f >> lgh, j = (f & ((L >> 1) - 1)) << 1;
+        const i64 rb = vi[b].rb_in;
+        const i64 r = rb + j;
+        E *d = sm + b * Lp + pidx<E>(j);
+        const E *s = src + vi[b].col_src + r;
+        if (rb >= 0 && j + 1 < in_len && r + 1 < in_rows &&
+            (((size_t)s & 15) == 0)) {
+          cp_async<16>(d, s, true);
+        } else {
+          const bool ok0 = rb >= 0 && j < in_len && r < in_rows;
+          const bool ok1 = rb >= 0 && j + 1 < in_len && r + 1 < in_rows;
+          cp_async<8>(d, ok0 ? (const void *)s : (const void *)src, ok0);
+          cp_async<8>(d + 1, ok1 ? (const void *)(s + 1) : (const void *)src,
+                      ok1);
+        }
+      }
+      return;
+    }
+  }
   Walk w(tid, L, T);
   for (int f = tid; f < total; f += T, w.next()) {
     int b, j;
@@ -1958,12 +1984,14 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
         __syncthreads();
       }
       const int nwarps = T >> 5;
-      bool natural = false;
+      bool natural = false, stored = false;
       if constexpr (std::is_same<E, float2>::value) {
         if (p.rprog) {
-          // the program on registers; results in natural order
+          // the program on registers; results in natural order (or already
+          // stored)
           rt_program(p, sm, vi, tid, T);
           natural = true;
+          stored = (p.rprog & RT_DIRECT) != 0;
         }
       }
       if (natural) {
@@ -1975,7 +2003,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       } else {
         run_program<E, CLS, 0>(p, sm, p.Lp, p.B, vi, sq, tid, T);
       }
-      store_tile<E, 0>(p, sm, vi, sexp, tid, T, natural);
+      if (!stored) store_tile<E, 0>(p, sm, vi, sexp, tid, T, natural);
       __syncthreads();
       cur ^= 1;
       kc = kn;
