@@ -1281,6 +1281,25 @@ __device__ __forceinline__ void load_async(const Step &p, E *sm,
       return;
     }
   }
+  if (LAY == 0 && cc > 1 && B <= T) {
+    // vectors strided across rows: consecutive threads take consecutive
+    // vectors, so (T a multiple of B) each thread keeps one vector and
+    // walks its points
+    const int b = tid & (B - 1);
+    const i64 rb = vi[b].rb_in;
+    const E *s = src + vi[b].col_src + rb;
+    E *d = sm + b * Lp;
+    const int js = T >> lgB;
+    const i64 lim = rb >= 0 ? in_rows - rb : 0;
+    for (int j = tid >> lgB; j < L; j += js) {
+      const i64 off = (i64)j * cc;
+      const bool ok = j < in_len && off < lim;
+      cp_async<sizeof(E)>(d + pidx<E>(j), ok ? (const void *)(s + off)
+                                             : (const void *)src,
+                          ok);
+    }
+    return;
+  }
   Walk w(tid, L, T);
   for (int f = tid; f < total; f += T, w.next()) {
     int b, j;
@@ -1458,6 +1477,36 @@ __device__ __forceinline__ void store_tile(const Step &p, const E *sm,
   const bool raw = p.dst_type == Tr<E>::code && !acc;
   void *const dst = p.dst;
   const int dst_type = p.dst_type;
+  if (LAY == 0 && ccout > 1 && B <= T && !map_out) {
+    // one vector per thread (T a multiple of B), its points j, j + T / B, ..
+    const int b = tid & (B - 1);
+    const i64 rb = vi[b].rb_out;
+    if (rb < 0) return;
+    const E *vsm = sm + b * Lp;
+    const i64 lim = out_rows - rb;
+    const i64 base = vi[b].col_dst + rb;
+    const int js = T >> lgB;
+    for (int j = tid >> lgB; j < out_len; j += js) {
+      const i64 off = (i64)j * ccout;
+      if (off >= lim) break;
+      E val = vsm[pidx<E>(out_pos ? out_pos[j] : j)];
+      if (post) val = mulv(val, post[rb + off], false);
+      if (has_scale) val = mulv(val, c, false);
+      if (conj_out) val = conjv(val);
+      if constexpr (Emu<E>::v) {
+        if (raw)
+          ((E *)dst)[base + off] = to_bits(val, sexp[b]);
+        else
+          store_as<E>(dst, dst_type, base + off, val, acc, sexp[b]);
+      } else {
+        if (raw)
+          ((E *)dst)[base + off] = val;
+        else
+          store_as<E>(dst, dst_type, base + off, val, acc);
+      }
+    }
+    return;
+  }
   Walk w(tid, out_len, T);
   for (int f = tid; f < total; f += T, w.next()) {
     int b, j;
