@@ -96,12 +96,19 @@ __device__ __forceinline__ int rt_nat(int p) {
   return rt_nat_from<L, 0>(p, 0);
 }
 
+// barrier of the threads of one vector: the warp, or for L = 512 the pair
+// of warps (named barrier 1 + pair index; the CTA has 16 warps, so ids
+// 1..8), or the CTA beyond
 template <int L>
 __device__ __forceinline__ void rt_sync() {
-  if constexpr (L / kRtP > 32)
-    __syncthreads();  // a vector spans several warps
-  else
+  constexpr int G = L / kRtP;
+  if constexpr (G <= 32)
     __syncwarp();
+  else if constexpr (G == 64)
+    asm volatile("bar.sync %0, 64;" ::"r"(1 + (int)(threadIdx.x >> 6))
+                 : "memory");
+  else
+    __syncthreads();
 }
 
 // stage I: DIF (DFT, then twiddles of the outputs) or DIT (twiddles of the
