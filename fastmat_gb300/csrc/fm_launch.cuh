@@ -68,6 +68,8 @@ cudaError_t launch_rconv(int ctype, const RcStep &p, cudaStream_t s);
 // lengths it is built for (powers of two; 0: not for this type), one launch
 int rfwht_min_len(int ctype);
 int rfwht_max_len(int ctype);
+int rsfwht_min_len(int ctype);  // strided vectors (element stride % 32 == 0)
+int rsfwht_max_len(int ctype);
 cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s);
 
 // largest FFT radix the kernels of a compute type are built with (see

@@ -254,6 +254,11 @@ struct LStep {
   // program (run by batches, and by kind 3 when the buffers do not suit it)
   int kind = 0;
   int rc_L = 0;
+  // kind 3: the real type the FWHT kernel runs in (complex data as pairs
+  // of real vectors), and for strided vectors their element stride, count
+  // per column and column strides in real words (0: contiguous kernel)
+  int rc_ct = 0;
+  i64 rc_es = 0, rc_A = 0, rc_ld_src = 0, rc_ld_dst = 0;
   const void *rc_spec = nullptr, *rc_tw = nullptr;  // spectrum in rconv order
   const void *rc_pre = nullptr, *rc_post = nullptr;
   int rc_conj_in = 0, rc_conj_out = 0, rc_spec_conj = 0;
@@ -1628,24 +1633,47 @@ class Planner {
     ls.kind = 2;
   }
 
-  // A program that is one FWHT over contiguous whole vectors of real data,
-  // with a length the register FWHT is built for, runs there (kind 3).
+  // A program that is one FWHT over whole vectors, with a length the
+  // register FWHTs are built for, runs there (kind 3): contiguous vectors
+  // of real data (rfwht_kernel), or vectors at an element stride that is a
+  // multiple of 32 (rsfwht_kernel), real or complex (the real and imaginary
+  // parts of complex vectors at stride S are real vectors at stride 2 S).
+  // The tensor-core form of the FWHT (FM_F32_TC) runs in these kernels as
+  // well: the transform is bound by HBM traffic, which they reach on the
+  // FP32 pipes.
   void try_rfwht(LStep &ls, const std::vector<fmk::Op> &ops) {
-    const int ct = P_->ctype;
+    const int ct0 = P_->ctype;
+    const bool cx = ct0 == FM_C64 || ct0 == FM_C128_DF;
+    const int ct = (ct0 == FM_C64 || ct0 == FM_F32_TC)
+                       ? FM_F32
+                       : ct0 == FM_C128_DF ? FM_F64_DF : ct0;
     const fmk::Step &st = ls.st;
-    const int lmin = fmk::rfwht_min_len(ct), lmax = fmk::rfwht_max_len(ct);
-    if (!lmax || ops.size() != 1 || ops[0].kind != fmk::OP_FWHT ||
-        ops[0].sign != 0)
+    if (ops.size() != 1 || ops[0].kind != fmk::OP_FWHT ||
+        (ops[0].sign != 0 && ct0 != FM_F32_TC))
       return;
     const int L = ops[0].len;
-    if (!is_pow2(L) || L < lmin || L > lmax || st.L != L) return;
-    if (st.vin.Cc != 1 || st.vout.Cc != 1 || st.vin.n != L ||
-        st.vout.n != L || st.vin.A != st.vout.A || st.in_len != L ||
-        st.out_len != L || st.in_rows != st.vin.A * L ||
-        st.out_rows != st.vout.A * L || st.map_in || st.map_out ||
-        st.out_mode || st.pre || st.post || st.conj_in || st.conj_out ||
-        st.has_scale || st.accumulate)
+    if (!is_pow2(L) || st.L != L) return;
+    if (st.vin.A != st.vout.A || st.vin.n != L || st.vout.n != L ||
+        st.vin.Cc != st.vout.Cc || st.in_len != L || st.out_len != L ||
+        st.in_rows != st.vin.A * L * st.vin.Cc ||
+        st.out_rows != st.vout.A * L * st.vout.Cc || st.map_in ||
+        st.map_out || st.out_mode || st.pre || st.post || st.conj_in ||
+        st.conj_out || st.has_scale || st.accumulate)
       return;
+    const i64 S = st.vin.Cc;
+    if (S == 1) {
+      if (cx || L < fmk::rfwht_min_len(ct) || L > fmk::rfwht_max_len(ct))
+        return;
+      ls.rc_es = 0;
+    } else {
+      if (S % 32 || L < fmk::rsfwht_min_len(ct) ||
+          L > fmk::rsfwht_max_len(ct))
+        return;
+      const int k = cx ? 2 : 1;  // real words per element
+      ls.rc_es = S * k;
+      ls.rc_A = st.vin.A * S * k;
+    }
+    ls.rc_ct = ct;
     ls.rc_L = L;
     ls.kind = 3;
   }
@@ -2069,27 +2097,32 @@ bool encode_view(CUtensorMap *tm, const void *base, const fmk::View &vw,
 // Finish a bound launch (TMA descriptors, status word) and issue it.
 void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
   if (ls.kind == 3) {
-    // raw buffers of the I/O type, 16-byte aligned columns and vectors
+    // raw buffers of the I/O type; the contiguous kernel also wants
+    // 16-byte aligned columns and vectors
     const int esz = esize(P->io_type);
+    const bool strided = ls.rc_es > 1;
     const bool fit = st.src_type == P->io_type && st.dst_type == P->io_type &&
-                     ((uintptr_t)st.src & 15) == 0 &&
-                     ((uintptr_t)st.dst & 15) == 0 &&
-                     (st.ld_src * esz) % 16 == 0 &&
-                     (st.ld_dst * esz) % 16 == 0 && !st.accumulate;
+                     !st.accumulate &&
+                     (strided || (((uintptr_t)st.src & 15) == 0 &&
+                                  ((uintptr_t)st.dst & 15) == 0 &&
+                                  (st.ld_src * esz) % 16 == 0 &&
+                                  (st.ld_dst * esz) % 16 == 0));
     if (fit) {
       fmk::RfStep rf;
+      const int k = strided ? (int)(ls.rc_es / st.vin.Cc) : 1;
       rf.src = st.src;
       rf.dst = st.dst;
-      rf.ld_src = st.ld_src;
-      rf.ld_dst = st.ld_dst;
-      rf.A = st.vin.A;
+      rf.ld_src = st.ld_src * k;
+      rf.ld_dst = st.ld_dst * k;
+      rf.A = strided ? ls.rc_A : st.vin.A;
       rf.stride = st.vin.n;
+      rf.es = strided ? ls.rc_es : 1;
       rf.num_cols = st.num_cols;
       rf.err = P->err;
       rf.L = ls.rc_L;
-      if (rf.A * rf.num_cols >= 0x7fffffffLL)
+      if (rf.A * rf.num_cols >= 0x7fffffffLL || rf.es >= 0x7fffffffLL)
         fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
-      CUDA_TRY(fmk::launch_rfwht(P->ctype, rf, s));
+      CUDA_TRY(fmk::launch_rfwht(ls.rc_ct, rf, s));
       return;
     }
     // otherwise the equivalent vector program below
@@ -2897,9 +2930,11 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
       if (ls.kind == 3) {
         snprintf(line, sizeof(line),
                  "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,"
-                 "%lld) rfwht L=%d acc=%d: fwht(%d)\n",
+                 "%lld) rfwht L=%d stride=%lld acc=%d: fwht(%d)\n",
                  ls.src, ls.dst, st.vin.A, st.vin.n, st.vin.Cc, st.vout.A,
-                 st.vout.n, st.vout.Cc, ls.rc_L, st.accumulate, ls.rc_L);
+                 st.vout.n, st.vout.Cc, ls.rc_L,
+                 (long long)(ls.rc_es > 1 ? ls.rc_es : 1), st.accumulate,
+                 ls.rc_L);
         s += line;
         continue;
       }

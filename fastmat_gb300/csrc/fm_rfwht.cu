@@ -1,6 +1,7 @@
-// Instantiations and launcher of the register-resident FWHT kernel
+// Instantiations and launchers of the register-resident FWHT kernels
 // (fm_rfwht.cuh): float32 and double-float real data, contiguous vectors of
-// 1024..8192 (float32) or 256..8192 (double-float) points.
+// 1024..8192 (float32) or 256..8192 (double-float) points, strided vectors
+// of 64..1024 (float32) or 32..512 (double-float) points.
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -48,7 +49,49 @@ cudaError_t launch_one(const RfStep &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <class E, int L>
+cudaError_t launch_strided(const RfStep &p, cudaStream_t s) {
+  auto *fn = rsfwht_kernel<E, L>;
+  constexpr size_t smem = rs_smem<E, L>();
+  constexpr int T = RsShape<E, L>::T;
+  static std::mutex mu;
+  static std::map<int, int> resident;  // device -> CTAs per SM x SMs
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int cap = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find(dev);
+    if (it == resident.end()) {
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, sms = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      it = resident.emplace(dev, (per_sm < 1 ? 1 : per_sm) * sms).first;
+    }
+    cap = it->second;
+  }
+  const long long nb = (long long)p.A * p.num_cols / 32;
+  long long grid = nb;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  fn<<<(unsigned)grid, T, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+int rsfwht_min_len(int ctype) {
+  return ctype == FM_F32 ? 64 : ctype == FM_F64_DF ? 32 : 0;
+}
+int rsfwht_max_len(int ctype) {
+  return ctype == FM_F32 ? 1024 : ctype == FM_F64_DF ? 512 : 0;
+}
 
 int rfwht_min_len(int ctype) {
   return ctype == FM_F32 ? 1024 : ctype == FM_F64_DF ? 256 : 0;
@@ -58,6 +101,28 @@ int rfwht_max_len(int ctype) {
 }
 
 cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s) {
+  if (p.es > 1) {
+    if (ctype == FM_F32) {
+      switch (p.L) {
+        case 64: return launch_strided<float, 64>(p, s);
+        case 128: return launch_strided<float, 128>(p, s);
+        case 256: return launch_strided<float, 256>(p, s);
+        case 512: return launch_strided<float, 512>(p, s);
+        case 1024: return launch_strided<float, 1024>(p, s);
+        default: break;
+      }
+    } else if (ctype == FM_F64_DF) {
+      switch (p.L) {
+        case 32: return launch_strided<df, 32>(p, s);
+        case 64: return launch_strided<df, 64>(p, s);
+        case 128: return launch_strided<df, 128>(p, s);
+        case 256: return launch_strided<df, 256>(p, s);
+        case 512: return launch_strided<df, 512>(p, s);
+        default: break;
+      }
+    }
+    return cudaErrorInvalidConfiguration;
+  }
   if (ctype == FM_F32) {
     switch (p.L) {
       case 1024: return launch_one<float, 1024>(p, s);

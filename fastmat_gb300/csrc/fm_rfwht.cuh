@@ -41,7 +41,9 @@ struct RfStep {
   void *dst;
   i64 ld_src, ld_dst;
   i64 A;       // vectors per column
-  i64 stride;  // rows from one vector of a column to the next
+  i64 stride;  // contiguous vectors: rows from one vector to the next
+  i64 es;      // element stride: 1 contiguous vectors; S > 1: vector
+               // v = a S + c has point j at row a L S + c + j S
   i64 num_cols;
   int *err;
   int L;
@@ -259,6 +261,92 @@ __global__ void __launch_bounds__(RfShape<E, L>::T, (RfOcc<E, L>::v))
     }
   }
   cp_async_wait<0>();
+}
+
+// ---- strided vectors (the high index bits of a long transform: vectors
+// of L points at element stride S, S a multiple of 32, adjacent vectors
+// adjacent in memory).  The 32 lanes of a warp take 32 adjacent vectors, so
+// every load and store of a warp is one contiguous row segment; the L / P
+// warps of the CTA share the vectors' points, thread (lane v, warp t) the
+// same points t P .. t P + P - 1 of vector v as thread t of the contiguous
+// kernel, and the passes run as there (the exchanges go through a buffer per
+// vector whose odd stride keeps the 32 lanes on distinct banks).  The first
+// pass loads straight from global memory (P independent loads per thread),
+// the last stores straight to it.
+template <class E, int L> struct RsShape {
+  static constexpr int P = RfLane<E>::P;
+  static constexpr int W = L / P;  // warps per CTA = threads per vector
+  static constexpr int T = 32 * W;
+  static constexpr int Lx = (L + (L >> RfLane<E>::XSH)) | 1;
+};
+template <class E, int L>
+__host__ __device__ constexpr size_t rs_smem() {
+  return (size_t)32 * RsShape<E, L>::Lx * sizeof(E) + 32 * sizeof(int);
+}
+template <class E, int L> struct RsOcc {
+  static constexpr int v =
+      RsShape<E, L>::T >= 1024 ? 1 : 1024 / RsShape<E, L>::T;
+};
+
+template <class E, int L>
+__global__ void __launch_bounds__(RsShape<E, L>::T, (RsOcc<E, L>::v))
+    rsfwht_kernel(const __grid_constant__ RfStep p) {
+  typedef RsShape<E, L> Sh;
+  typedef typename RfLane<E>::Raw Raw;
+  constexpr int P = Sh::P, W = Sh::W;
+  static_assert(W >= 2 && W <= 32, "warps per CTA");
+  constexpr int SL = rf_last<E, L>();
+  constexpr int WL = rf_log2(L) - SL;
+  extern __shared__ __align__(128) unsigned char fm_smem[];
+  E *xb = reinterpret_cast<E *>(fm_smem);
+  int *sexp = reinterpret_cast<int *>(xb + 32 * Sh::Lx);
+  const int v = threadIdx.x & 31, t = threadIdx.x >> 5;
+  E *buf = xb + v * Sh::Lx;
+  const i64 S = p.es;
+  const i64 nb = p.A * p.num_cols / 32;  // batches of 32 adjacent vectors
+  const FDiv dA((unsigned)p.A), dS((unsigned)S);
+  for (i64 bt = blockIdx.x; bt < nb; bt += gridDim.x) {
+    const unsigned gv = (unsigned)(bt * 32);
+    const unsigned m = dA.div(gv), v0 = gv - m * (unsigned)p.A;
+    const unsigned a = dS.div(v0), c0 = v0 - a * (unsigned)S;
+    const i64 row0 = (i64)a * L * S + c0 + v;
+    const Raw *src = (const Raw *)p.src + (i64)m * p.ld_src + row0;
+    Raw d[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) d[r] = src[(i64)(t * P + r) * S];
+    E x[P];
+    int s = 0;
+    if constexpr (Emu<E>::v) {
+      // double-float: each vector scaled by the power of two of its largest
+      // exponent (float's exponent range), restored on store
+      int emax = 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) emax = max(emax, dexp(d[r]));
+      if (threadIdx.x < 32) sexp[threadIdx.x] = 0;
+      __syncthreads();
+      if (emax > 0) atomicMax(sexp + v, emax);
+      __syncthreads();
+      s = sexp[v] > 0 ? sexp[v] - 1023 : 0;
+#pragma unroll
+      for (int r = 0; r < P; ++r) x[r] = d2df_scaled(d[r], s);
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; ++r) x[r] = d[r];
+    }
+    // (W >= 2: the passes hold at least one exchange, whose barriers also
+    // separate this batch's reads of sexp from the next batch's reset)
+    rf_passes<E, L, 0>(x, buf, t);
+    Raw *dst = (Raw *)p.dst + (i64)m * p.ld_dst + row0;
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const int u = j >> WL, r = j & ((1 << WL) - 1);
+      const int e = rf_pos(t + W * u, SL, r, WL);
+      if constexpr (Emu<E>::v)
+        dst[(i64)e * S] = df2d_scaled(x[j], s);
+      else
+        dst[(i64)e * S] = x[j];
+    }
+  }
 }
 
 }  // namespace fmk
