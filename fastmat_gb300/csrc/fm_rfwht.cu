@@ -1,7 +1,7 @@
 // Instantiations and launchers of the register-resident FWHT kernels
 // (fm_rfwht.cuh): float32 and double-float real data, contiguous vectors of
 // 1024..8192 (float32) or 256..8192 (double-float) points, strided vectors
-// of 64..1024 (float32) or 32..512 (double-float) points.
+// of 64..2048 (float32) or 32..1024 (double-float) points.
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -76,7 +76,7 @@ cudaError_t launch_strided(const RfStep &p, cudaStream_t s) {
     }
     cap = it->second;
   }
-  const long long nb = (long long)p.A * p.num_cols / 32;
+  const long long nb = (long long)p.A * p.num_cols / RsShape<E, L>::NV;
   long long grid = nb;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
@@ -90,7 +90,7 @@ int rsfwht_min_len(int ctype) {
   return ctype == FM_F32 ? 64 : ctype == FM_F64_DF ? 32 : 0;
 }
 int rsfwht_max_len(int ctype) {
-  return ctype == FM_F32 ? 1024 : ctype == FM_F64_DF ? 512 : 0;
+  return ctype == FM_F32 ? 2048 : ctype == FM_F64_DF ? 1024 : 0;
 }
 
 int rfwht_min_len(int ctype) {
@@ -109,6 +109,7 @@ cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s) {
         case 256: return launch_strided<float, 256>(p, s);
         case 512: return launch_strided<float, 512>(p, s);
         case 1024: return launch_strided<float, 1024>(p, s);
+        case 2048: return launch_strided<float, 2048>(p, s);
         default: break;
       }
     } else if (ctype == FM_F64_DF) {
@@ -118,6 +119,7 @@ cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s) {
         case 128: return launch_strided<df, 128>(p, s);
         case 256: return launch_strided<df, 256>(p, s);
         case 512: return launch_strided<df, 512>(p, s);
+        case 1024: return launch_strided<df, 1024>(p, s);
         default: break;
       }
     }

@@ -265,23 +265,26 @@ __global__ void __launch_bounds__(RfShape<E, L>::T, (RfOcc<E, L>::v))
 
 // ---- strided vectors (the high index bits of a long transform: vectors
 // of L points at element stride S, S a multiple of 32, adjacent vectors
-// adjacent in memory).  The 32 lanes of a warp take 32 adjacent vectors, so
-// every load and store of a warp is one contiguous row segment; the L / P
-// warps of the CTA share the vectors' points, thread (lane v, warp t) the
-// same points t P .. t P + P - 1 of vector v as thread t of the contiguous
-// kernel, and the passes run as there (the exchanges go through a buffer per
-// vector whose odd stride keeps the 32 lanes on distinct banks).  The first
-// pass loads straight from global memory (P independent loads per thread),
-// the last stores straight to it.
+// adjacent in memory).  The lanes of a warp take NV = 32 (or, for vectors
+// of more than 32 P points, 16) adjacent vectors, so every load and store of
+// a warp is one or two contiguous row segments; the CTA's threads share the
+// vectors' points, thread t of vector v (t = warp (32 / NV) + lane / NV)
+// holding points t P .. t P + P - 1 as thread t of the contiguous kernel,
+// and the passes run as there (the exchanges go through a buffer per vector
+// whose odd stride keeps the lanes of each half-warp on distinct banks).
+// The first pass loads straight from global memory (P independent loads per
+// thread), the last stores straight to it.
 template <class E, int L> struct RsShape {
   static constexpr int P = RfLane<E>::P;
-  static constexpr int W = L / P;  // warps per CTA = threads per vector
-  static constexpr int T = 32 * W;
+  static constexpr int W = L / P;             // threads per vector
+  static constexpr int NV = W > 32 ? 16 : 32;  // vectors per CTA batch
+  static constexpr int T = NV * W;
   static constexpr int Lx = (L + (L >> RfLane<E>::XSH)) | 1;
 };
 template <class E, int L>
 __host__ __device__ constexpr size_t rs_smem() {
-  return (size_t)32 * RsShape<E, L>::Lx * sizeof(E) + 32 * sizeof(int);
+  return (size_t)RsShape<E, L>::NV * RsShape<E, L>::Lx * sizeof(E) +
+         32 * sizeof(int);
 }
 template <class E, int L> struct RsOcc {
   static constexpr int v =
@@ -293,20 +296,22 @@ __global__ void __launch_bounds__(RsShape<E, L>::T, (RsOcc<E, L>::v))
     rsfwht_kernel(const __grid_constant__ RfStep p) {
   typedef RsShape<E, L> Sh;
   typedef typename RfLane<E>::Raw Raw;
-  constexpr int P = Sh::P, W = Sh::W;
-  static_assert(W >= 2 && W <= 32, "warps per CTA");
+  constexpr int P = Sh::P, W = Sh::W, NV = Sh::NV;
+  static_assert(W >= 2 && Sh::T <= 1024, "threads per CTA");
   constexpr int SL = rf_last<E, L>();
   constexpr int WL = rf_log2(L) - SL;
   extern __shared__ __align__(128) unsigned char fm_smem[];
   E *xb = reinterpret_cast<E *>(fm_smem);
-  int *sexp = reinterpret_cast<int *>(xb + 32 * Sh::Lx);
-  const int v = threadIdx.x & 31, t = threadIdx.x >> 5;
+  int *sexp = reinterpret_cast<int *>(xb + NV * Sh::Lx);
+  const int lane = threadIdx.x & 31;
+  const int v = lane % NV;
+  const int t = (threadIdx.x >> 5) * (32 / NV) + lane / NV;
   E *buf = xb + v * Sh::Lx;
   const i64 S = p.es;
-  const i64 nb = p.A * p.num_cols / 32;  // batches of 32 adjacent vectors
+  const i64 nb = p.A * p.num_cols / NV;  // batches of NV adjacent vectors
   const FDiv dA((unsigned)p.A), dS((unsigned)S);
   for (i64 bt = blockIdx.x; bt < nb; bt += gridDim.x) {
-    const unsigned gv = (unsigned)(bt * 32);
+    const unsigned gv = (unsigned)(bt * NV);
     const unsigned m = dA.div(gv), v0 = gv - m * (unsigned)p.A;
     const unsigned a = dS.div(v0), c0 = v0 - a * (unsigned)S;
     const i64 row0 = (i64)a * L * S + c0 + v;
@@ -322,7 +327,7 @@ __global__ void __launch_bounds__(RsShape<E, L>::T, (RsOcc<E, L>::v))
       int emax = 0;
 #pragma unroll
       for (int r = 0; r < P; ++r) emax = max(emax, dexp(d[r]));
-      if (threadIdx.x < 32) sexp[threadIdx.x] = 0;
+      if (threadIdx.x < NV) sexp[threadIdx.x] = 0;
       __syncthreads();
       if (emax > 0) atomicMax(sexp + v, emax);
       __syncthreads();

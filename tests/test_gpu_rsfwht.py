@@ -41,7 +41,7 @@ def test_long_hadamard_float32_bit_exact(order):
 
 
 @pytest.mark.parametrize('order,strided', [(18, True), (20, True),
-                                           (22, None)])
+                                           (22, True)])
 def test_long_hadamard_double_float(order, strided):
     import fastmat_gb300 as fg
     rng = np.random.default_rng(order + 7)
@@ -56,7 +56,7 @@ def test_long_hadamard_double_float(order, strided):
 
 
 @pytest.mark.parametrize('k,m', [(6, 32), (7, 64), (8, 128), (9, 32),
-                                 (10, 64), (5, 96)])
+                                 (10, 64), (11, 32), (12, 32), (5, 96)])
 @pytest.mark.parametrize('dtype', [np.float32, np.float64])
 def test_kron_hadamard_mode_real(k, m, dtype):
     """Kron(Hadamard(k), Eye(m)): 2^k points at stride m."""
@@ -66,7 +66,7 @@ def test_kron_hadamard_mode_real(k, m, dtype):
     oop = fo.Kron(fo.Hadamard(k), fo.Eye(m))
     n = (1 << k) * m
     x = rng.standard_normal((n, 3)).astype(dtype)
-    lo, hi = (64, 1024) if dtype == np.float32 else (32, 512)
+    lo, hi = (64, 2048) if dtype == np.float32 else (32, 1024)
     assert bool(_strided_fwht(op, dtype)) == (lo <= (1 << k) <= hi)
     y = op.forward(x)
     assert y.dtype == dtype
