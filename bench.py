@@ -358,8 +358,14 @@ def roofline_of(fg, plan, per_launch, n_in, n_out, M, dt, out_dt, peak,
                n_out * np.dtype(out_dt).itemsize) * M] * len(per_launch)
     k = int(np.argmax(per_launch))
     ach = lb[k] / (per_launch[k] * 1e-3) / 1e9
-    kernel = 'rconv' if 'rconv' in plan.describe(0).splitlines()[k] \
-        else what
+    line = [ln for ln in plan.describe(0).splitlines()
+            if ln.startswith('launch')][k]
+    if 'rconv' in line:
+        kernel = 'rconv'
+    elif 'rfwht' in line:
+        kernel = 'rfwht' if 'stride=1 ' in line else 'rsfwht'
+    else:
+        kernel = what
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_kind": peak_kind,
             "traffic": ncu_traffic(workload, form, k + 1),
@@ -658,7 +664,8 @@ def run_gpu(args):
             "unit": "GB/s", "ms_per_step": r32['ms'],
             "speedup_vs_fp64": r64['ms'] / r32['ms'],
             "rel_err_vs_oracle": rel32, "rel_err_vs_fp64": rel32_64,
-            "dtype": "c64", "roofline": r32['roofline']},
+            "dtype": "c64" if np.dtype(dt64).kind == 'c' else "f32",
+            "roofline": r32['roofline']},
         "roofline": r64['roofline'],
         "e2e": e2e,
         "gpu_launches": int(args.steps * r64['n_launch']),

@@ -70,6 +70,9 @@ int rfwht_min_len(int ctype);
 int rfwht_max_len(int ctype);
 int rsfwht_min_len(int ctype);  // strided vectors (element stride % 32 == 0)
 int rsfwht_max_len(int ctype);
+// both passes of a two-pass FWHT in one launch (rfwht2_kernel)
+bool rfwht2_supported(int ctype, int L1, int L2);
+cudaError_t launch_rfwht2(int ctype, const RfPair &p, cudaStream_t s);
 cudaError_t launch_rfwht(int ctype, const RfStep &p, cudaStream_t s);
 
 // largest FFT radix the kernels of a compute type are built with (see

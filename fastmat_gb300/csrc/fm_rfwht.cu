@@ -84,7 +84,81 @@ cudaError_t launch_strided(const RfStep &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <class E, int L1, int L2>
+cudaError_t launch_pair(const RfPair &p, cudaStream_t s) {
+  auto *fn = rfwht2_kernel<E, L1, L2>;
+  constexpr size_t smem = rf2_smem<E, L1, L2>();
+  static std::mutex mu;
+  static std::map<int, int> resident;  // device -> CTAs per SM x SMs
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int cap = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find(dev);
+    if (it == resident.end()) {
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, sms = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, fn, FM_RF2_THREADS, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      it = resident.emplace(dev, per_sm * sms).first;
+    }
+    cap = it->second;
+  }
+  if (cap < 1) return cudaErrorInvalidConfiguration;
+  // every CTA resident at once (cooperative): the waits of the second pass
+  // rely on it
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cap);
+  cfg.blockDim = dim3(FM_RF2_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, p);
+}
+
 }  // namespace
+
+bool rfwht2_supported(int ctype, int L1, int L2) {
+  if (ctype == FM_F32)
+    return L1 == 8192 && (L2 == 64 || L2 == 128 || L2 == 256 || L2 == 512);
+  if (ctype == FM_F64_DF)
+    return L1 == 4096 && L2 >= 32 && L2 <= 1024 && (L2 & (L2 - 1)) == 0;
+  return false;
+}
+
+cudaError_t launch_rfwht2(int ctype, const RfPair &p, cudaStream_t s) {
+  if (ctype == FM_F32 && p.a.L == 8192) {
+    switch (p.b.L) {
+      case 64: return launch_pair<float, 8192, 64>(p, s);
+      case 128: return launch_pair<float, 8192, 128>(p, s);
+      case 256: return launch_pair<float, 8192, 256>(p, s);
+      case 512: return launch_pair<float, 8192, 512>(p, s);
+      default: break;
+    }
+  } else if (ctype == FM_F64_DF && p.a.L == 4096) {
+    switch (p.b.L) {
+      case 32: return launch_pair<df, 4096, 32>(p, s);
+      case 64: return launch_pair<df, 4096, 64>(p, s);
+      case 128: return launch_pair<df, 4096, 128>(p, s);
+      case 256: return launch_pair<df, 4096, 256>(p, s);
+      case 512: return launch_pair<df, 4096, 512>(p, s);
+      case 1024: return launch_pair<df, 4096, 1024>(p, s);
+      default: break;
+    }
+  }
+  return cudaErrorInvalidConfiguration;
+}
 
 int rsfwht_min_len(int ctype) {
   return ctype == FM_F32 ? 64 : ctype == FM_F64_DF ? 32 : 0;

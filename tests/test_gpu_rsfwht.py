@@ -35,9 +35,29 @@ def test_long_hadamard_float32_bit_exact(order):
     x = rng.standard_normal((1 << order, 2)).astype(np.float32)
     H = fg.Hadamard(order)
     assert _strided_fwht(H, np.float32)
+    # both passes in one launch, column by column
+    assert 'fused-with-next' in H.plan(np.float32).describe(0)
     y = H.forward(x)
     _same(y, fo.Hadamard(order).forward(x))
     _same(H.backward(x), y)
+
+
+def test_fused_passes_many_columns_and_leading_dimension():
+    """The fused two-pass launch over 70 columns with a padded leading
+    dimension (the column counters and the column-by-column order), float32
+    bit-exact."""
+    import torch
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(70)
+    n = 1 << 19
+    big = torch.from_numpy(rng.standard_normal((70, n + 4)).astype(
+        np.float32)).cuda()
+    xt = big[:, :n].t()                  # leading dimension n + 4
+    H = fg.Hadamard(19)
+    y = H.forward(xt).cpu().numpy()
+    pick = [0, 1, 34, 69]
+    x = xt.cpu().numpy()
+    _same(y[:, pick], fo.Hadamard(19).forward(np.asfortranarray(x[:, pick])))
 
 
 @pytest.mark.parametrize('order,strided', [(18, True), (20, True),
@@ -50,6 +70,7 @@ def test_long_hadamard_double_float(order, strided):
     H = fg.Hadamard(order)
     if strided:
         assert _strided_fwht(H, np.float64)
+        assert 'fused-with-next' in H.plan(np.float64).describe(0)
     y = H.forward(x)
     assert y.dtype == np.float64
     assert fo.rel_err(y, fo.Hadamard(order).forward(x)) <= 1e-12
