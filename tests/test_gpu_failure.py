@@ -72,6 +72,43 @@ def test_wait_limit_zero_reports_timeout_then_recovers(expr):
         plan.set_wait_limit(-1)
 
 
+def test_fused_fwht_pass_wait_timeout_then_recovers():
+    """The fused two-pass FWHT (one launch, second-pass items wait for
+    their column's first-pass items): with the poll limit 0 a second-pass
+    item that finds its column unfinished gives up at once.  With one
+    column the second-pass items are handed out while the last first-pass
+    items still run, so a timeout is all but certain within three calls;
+    the kernel returns, check() reports it, and with the default limit the
+    result is bit-exact again."""
+    import torch
+    import fastmat_gb300 as fg
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((1 << 22, 1)).astype(np.float32)
+    xt = torch.from_numpy(np.ascontiguousarray(x.T)).cuda().t()
+    op = fg.Hadamard(22)
+    plan = op.plan(np.float32)
+    assert 'fused-with-next' in plan.describe(0)
+    plan.set_wait_limit(0)
+    timed_out = False
+    try:
+        for _ in range(3):
+            op.forward(xt)
+            try:
+                plan.check()
+            except RuntimeError as e:
+                assert 'bounded wait' in str(e)
+                timed_out = True
+                break
+    finally:
+        plan.set_wait_limit(1 << 22)
+    assert timed_out
+    plan.check()
+    y = op.forward(xt).cpu().numpy()
+    plan.check()
+    ref = fo.Hadamard(22).forward(x)
+    assert np.array_equal(y.view(np.uint32), ref.view(np.uint32))
+
+
 def test_batch_grid_barrier_timeout_then_recovers():
     import torch
     import fastmat_gb300 as fg
