@@ -7,6 +7,7 @@
 
 #include "fm_rconv.cuh"
 #include "fm_rfwht.cuh"
+#include "fm_rsfft.cuh"
 #include "fm_vprog.cuh"
 
 namespace fmk {
@@ -70,6 +71,10 @@ int rfwht_min_len(int ctype);
 int rfwht_max_len(int ctype);
 int rsfwht_min_len(int ctype);  // strided vectors (element stride % 32 == 0)
 int rsfwht_max_len(int ctype);
+// FFT of strided complex vectors (rsfft_kernel)
+int rsfft_min_len(int ctype);
+int rsfft_max_len(int ctype);
+cudaError_t launch_rsfft(int ctype, const RsfStep &p, cudaStream_t s);
 // both passes of a two-pass FWHT in one launch (rfwht2_kernel)
 bool rfwht2_supported(int ctype, int L1, int L2);
 cudaError_t launch_rfwht2(int ctype, const RfPair &p, cudaStream_t s);

@@ -250,8 +250,10 @@ struct LStep {
   i64 src_off = 0, dst_off = 0;
   // 0: vector program (vprog_kernel); 1: CSR sparse product (spmv_kernel);
   // 2: register-resident convolution (rconv_kernel), 3: register-resident
-  // FWHT (rfwht_kernel); for both `st` still holds the equivalent vector
-  // program (run by batches, and by kind 3 when the buffers do not suit it)
+  // FWHT (rfwht_kernel / rsfwht_kernel / rfwht2_kernel), 4: register FFT of
+  // strided vectors (rsfft_kernel); for 2..4 `st` still holds the
+  // equivalent vector program (run by batches, and when the buffers do not
+  // suit the register kernel)
   int kind = 0;
   int rc_L = 0;
   // kind 3: the real type the FWHT kernel runs in (complex data as pairs
@@ -264,6 +266,7 @@ struct LStep {
   // element stride and vectors per column in rc2_*), 2 on that strided pass
   int pair = 0;
   int rc2_L = 0;
+  int rc_sign = 0;  // kind 4: transform sign
   i64 rc2_es = 0, rc2_A = 0;
   const void *rc_spec = nullptr, *rc_tw = nullptr;  // spectrum in rconv order
   const void *rc_pre = nullptr, *rc_post = nullptr;
@@ -1725,10 +1728,37 @@ class Planner {
     ls.kind = 3;
   }
 
+  // A program that is one FFT over whole vectors at an element stride that
+  // is a multiple of 32 (a Fourier mode of a Kron), complex64 or
+  // double-float complex, with a length the strided register FFT is built
+  // for, runs there (kind 4).
+  void try_rsfft(LStep &ls, const std::vector<fmk::Op> &ops) {
+    const int ct = P_->ctype;
+    const fmk::Step &st = ls.st;
+    const int lmin = fmk::rsfft_min_len(ct), lmax = fmk::rsfft_max_len(ct);
+    if (!lmax || ops.size() != 1 || ops[0].kind != fmk::OP_FFT) return;
+    const int L = ops[0].len;
+    const i64 S = st.vin.Cc;
+    if (!is_pow2(L) || L < lmin || L > lmax || st.L != L || S % 32) return;
+    if (st.vin.A != st.vout.A || st.vin.n != L || st.vout.n != L ||
+        st.vout.Cc != S || st.in_len != L || st.out_len != L ||
+        st.in_rows != st.vin.A * L * S || st.out_rows != st.vout.A * L * S ||
+        st.map_in || st.map_out || st.out_mode || st.pre || st.post ||
+        st.conj_in || st.conj_out || st.has_scale || st.accumulate)
+      return;
+    ls.rc_L = L;
+    ls.rc_es = S;
+    ls.rc_A = st.vin.A * S;
+    ls.rc_tw = twiddle(L);
+    ls.rc_sign = ops[0].sign;
+    ls.kind = 4;
+  }
+
   void finish(LStep &ls, const std::vector<fmk::Op> &ops_in) {
     fmk::Step &st = ls.st;
     try_rconv(ls, ops_in);
     if (ls.kind == 0) try_rfwht(ls, ops_in);
+    if (ls.kind == 0) try_rsfft(ls, ops_in);
     std::vector<fmk::Op> ops = ops_in;
     st.out_pos = finalize(ops);
     if ((int)ops.size() > FM_MAX_OPS)
@@ -2197,6 +2227,29 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
         return;
       }
       CUDA_TRY(fmk::launch_rfwht(ls.rc_ct, rf, s));
+      return;
+    }
+    // otherwise the equivalent vector program below
+  }
+  if (ls.kind == 4) {
+    // raw buffers of the I/O type
+    if (st.src_type == P->io_type && st.dst_type == P->io_type &&
+        !st.accumulate) {
+      fmk::RsfStep rs;
+      rs.src = st.src;
+      rs.dst = st.dst;
+      rs.ld_src = st.ld_src;
+      rs.ld_dst = st.ld_dst;
+      rs.A = ls.rc_A;
+      rs.es = ls.rc_es;
+      rs.num_cols = st.num_cols;
+      rs.tw = ls.rc_tw;
+      rs.err = P->err;
+      rs.L = ls.rc_L;
+      rs.sign = ls.rc_sign;
+      if (rs.A * rs.num_cols >= 0x7fffffffLL || rs.es >= 0x7fffffffLL)
+        fail(FM_ERR_UNSUPPORTED, "more than 2^31 vectors in one launch");
+      CUDA_TRY(fmk::launch_rsfft(P->ctype, rs, s));
       return;
     }
     // otherwise the equivalent vector program below
@@ -3012,6 +3065,16 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
                  : ls.pair == 2 ? "fused-with-previous "
                                 : "",
                  st.accumulate, ls.rc_L);
+        s += line;
+        continue;
+      }
+      if (ls.kind == 4) {
+        snprintf(line, sizeof(line),
+                 "launch src=%d dst=%d in=(%lld,%lld,%lld) out=(%lld,%lld,"
+                 "%lld) rsfft L=%d stride=%lld acc=%d: fft(%d, sign %d)\n",
+                 ls.src, ls.dst, st.vin.A, st.vin.n, st.vin.Cc, st.vout.A,
+                 st.vout.n, st.vout.Cc, ls.rc_L, (long long)ls.rc_es,
+                 st.accumulate, ls.rc_L, ls.rc_sign);
         s += line;
         continue;
       }

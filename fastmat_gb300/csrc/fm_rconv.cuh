@@ -116,7 +116,7 @@ __host__ __device__ constexpr int rc_twlen() {  // entries of stages < I
 // or inverse (INV = true: conjugate twiddles of the inputs, then DFT with
 // sign +1) transform on the lane's P registers, in place: register
 // u R + r holds position base + u G R + M r before and after.
-template <class E, int L, int I, bool INV>
+template <class E, int L, int I, bool INV, int FSG = -1>
 __device__ __forceinline__ void rc_stage(E (&x)[RcLane<E>::P], int g,
                                          const E *__restrict__ stw) {
   constexpr int P = RcLane<E>::P;
@@ -125,7 +125,7 @@ __device__ __forceinline__ void rc_stage(E (&x)[RcLane<E>::P], int g,
   constexpr int M = Mprev / R;
   constexpr int NB = P / R;
   constexpr int TS = L / Mprev;  // table stride of w_Mprev
-  constexpr int SG = INV ? +1 : -1;
+  constexpr int SG = INV ? +1 : FSG;  // FSG: sign of a forward-order DIF
   typedef typename Lazy<E>::type LC;
   constexpr int G = L / P;
   // the twiddles w_Mprev^(t k), t = g mod M, k < R, are the same for all
@@ -152,7 +152,7 @@ __device__ __forceinline__ void rc_stage(E (&x)[RcLane<E>::P], int g,
       LC y = v[i];
       const int k = brev<R>(i);
       if constexpr (!INV && M > 1) {
-        if (k != 0) y = cmul_lazy<-1>(y, w[k]);
+        if (k != 0) y = cmul_lazy<FSG>(y, w[k]);
       }
       x[u * R + k] = from_lazy(y);
     }
@@ -179,7 +179,8 @@ __device__ __forceinline__ int rc_off(int j) {  // register j = u R + r
 
 // Registers laid out for stage IA -> shared buffer -> registers laid out
 // for stage IB (warp barriers: the lanes of a vector are in one warp).
-template <class E, int L, int IA, int IB>
+// (CTA: the threads of a vector span several warps, CTA barriers)
+template <class E, int L, int IA, int IB, bool CTA = false>
 __device__ __forceinline__ void rc_exchange(E (&x)[RcLane<E>::P], E *buf,
                                             int g) {
   constexpr int P = RcLane<E>::P;
@@ -187,22 +188,56 @@ __device__ __forceinline__ void rc_exchange(E (&x)[RcLane<E>::P], E *buf,
 #pragma unroll
   for (int j = 0; j < P; ++j)
     buf[rc_pad<E, L>(ba + rc_off<E, L, IA>(j))] = x[j];
-  __syncwarp();
+  if constexpr (CTA)
+    __syncthreads();
+  else
+    __syncwarp();
 #pragma unroll
   for (int j = 0; j < P; ++j)
     x[j] = buf[rc_pad<E, L>(bb + rc_off<E, L, IB>(j))];
-  __syncwarp();
+  if constexpr (CTA)
+    __syncthreads();
+  else
+    __syncwarp();
 }
 
-template <class E, int L, int I>
+template <class E, int L, int I, int FSG = -1, bool CTA = false>
 __device__ __forceinline__ void rc_forward(E (&x)[RcLane<E>::P], E *buf, int g,
                                            const E *stw) {
-  rc_stage<E, L, I, false>(x, g, stw);
+  rc_stage<E, L, I, false, FSG>(x, g, stw);
   constexpr int S = rc_stages(L, RcLane<E>::P);
   if constexpr (I + 1 < S) {
-    rc_exchange<E, L, I, I + 1>(x, buf, g);
-    rc_forward<E, L, I + 1>(x, buf, g, stw);
+    rc_exchange<E, L, I, I + 1, CTA>(x, buf, g);
+    rc_forward<E, L, I + 1, FSG, CTA>(x, buf, g, stw);
   }
+}
+
+// natural index of the forward transform's output position p (radices
+// (P, ..., rest), R_0 most significant in the position): its digits in
+// reverse
+template <class E, int L, int I>
+__host__ __device__ constexpr int rc_below() {  // bits of the digits > I
+  constexpr int P = RcLane<E>::P;
+  if constexpr (I + 1 >= rc_stages(L, P))
+    return 0;
+  else
+    return rc_log2(rc_radix(I + 1, L, P)) + rc_below<E, L, I + 1>();
+}
+template <class E, int L, int I>
+__device__ __forceinline__ int rc_nat_from(int p, int sh) {
+  constexpr int P = RcLane<E>::P;
+  if constexpr (I >= rc_stages(L, P)) {
+    return 0;
+  } else {
+    constexpr int BI = rc_log2(rc_radix(I, L, P));
+    constexpr int BELOW = rc_below<E, L, I>();
+    return (((p >> BELOW) & ((1 << BI) - 1)) << sh) |
+           rc_nat_from<E, L, I + 1>(p, sh + BI);
+  }
+}
+template <class E, int L>
+__device__ __forceinline__ int rc_nat(int p) {
+  return rc_nat_from<E, L, 0>(p, 0);
 }
 template <class E, int L, int I>
 __device__ __forceinline__ void rc_inverse(E (&x)[RcLane<E>::P], E *buf, int g,
