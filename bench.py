@@ -362,8 +362,12 @@ def roofline_of(fg, plan, per_launch, n_in, n_out, M, dt, out_dt, peak,
             if ln.startswith('launch')][k]
     if 'rconv' in line:
         kernel = 'rconv'
+    elif 'fused-with-next' in line:
+        kernel = 'rfwht2 (both FWHT passes, one launch)'
     elif 'rfwht' in line:
         kernel = 'rfwht' if 'stride=1 ' in line else 'rsfwht'
+    elif 'rsfft' in line:
+        kernel = 'rsfft'
     else:
         kernel = what
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",

@@ -41,11 +41,14 @@ def test_wait_limit_zero_reports_timeout_then_recovers(expr):
         dt = np.complex128
         x = cplx(rng, 1024, 64)
     elif expr == 'kron_strided':   # strided mode: TMA boxes + mbarrier
-        # complex64 throughout: the loads need no type conversion
-        op = fg.Kron(fg.Fourier(64), fg.Eye(256), precision='fp32')
-        oop = fo.Kron(fo.Fourier(64), fo.Eye(256))
+        # complex64 throughout: the loads need no type conversion; 1024
+        # points, above the strided register FFT's lengths (which has no
+        # spin waits), so the mode runs on element-major TMA tiles
+        op = fg.Kron(fg.Fourier(1024), fg.Eye(64), precision='fp32')
+        oop = fo.Kron(fo.Fourier(1024), fo.Eye(64))
         dt = np.complex64
         x = cplx(rng, op.numCols, 8).astype(np.complex64)
+        assert 'rsfft' not in op.plan(np.complex64).describe(0)
     else:
         # (the register-resident FWHT, which takes orders 10 to 13 on
         # float32, has no spin waits: its copies complete in hardware)
