@@ -538,6 +538,61 @@ bool configure(int esz, LStep &ls, int want_B, int want_nbuf,
   return true;
 }
 
+// The register tile program (fm_rtile.cuh) a complex64 batch step runs, or
+// 0 when its vector program is not one of the shapes it covers:
+// [zero pad] DIF(L) [twiddle] or [zero pad] DIF(L) product DIT(L) [twiddle],
+// L = 64 .. 512 with the radix sequence (8, 8, ..., rest).
+static int rtile_shape(const fmk::Step &st);
+// the launch's threads cover whole vectors of the register tile program
+static bool rtile_threads_ok(const LStep &ls) {
+  const int G = ls.st.L / fmk::kRtP;
+  return ls.lay == 0 && G >= 1 && ls.threads >= G && ls.threads % G == 0 &&
+         ls.threads <= FM_MAX_THREADS;
+}
+static int rtile_shape(const fmk::Step &st) {
+  const int L = st.L;
+  if (L != 64 && L != 128 && L != 256 && L != 512) return 0;
+  if (st.out_mode == 1 || st.nops < 1) return 0;
+  auto radices_ok = [&](const fmk::Op &op) {
+    if (op.len != L || op.nrad != fmk::rc_stages(L, fmk::kRtP)) return false;
+    for (int i = 0; i < op.nrad; ++i)
+      if (op.rad[i] != fmk::rc_radix(i, L, fmk::kRtP)) return false;
+    return true;
+  };
+  int f = 0, o = 0, end = st.nops;
+  if (st.ops[0].kind == fmk::OP_ZPAD) {
+    if (st.ops[0].len2 != L || st.ops[0].len > L) return 0;
+    f |= fmk::RT_ZPAD;
+    o = 1;
+  }
+  if (end > o + 1 && st.ops[end - 1].kind == fmk::OP_TW) {
+    const fmk::Op &t = st.ops[end - 1];
+    if (t.len != L || t.N <= 0 || t.div < 1 || t.mod < 1 || !t.ptr3)
+      return 0;
+    f |= fmk::RT_TW;
+    --end;
+  }
+  if (o >= end) return 0;
+  const fmk::Op &d = st.ops[o];
+  if (d.kind != fmk::OP_DIF || !radices_ok(d)) return 0;
+  if (end == o + 1) {
+    if ((f & fmk::RT_TW) && !st.ops[st.nops - 1].ptr2) return 0;
+    return f | fmk::RT_FFT | (d.sign > 0 ? fmk::RT_INV : 0);
+  }
+  if (end == o + 3 && st.ops[o + 1].kind == fmk::OP_MUL &&
+      st.ops[o + 1].len == L && st.ops[o + 1].div >= 1 &&
+      st.ops[o + 1].mod >= 1 && st.ops[o + 2].kind == fmk::OP_DIT &&
+      radices_ok(st.ops[o + 2]) && d.sign < 0 && st.ops[o + 2].sign > 0) {
+    if ((f & fmk::RT_TW) && st.ops[st.nops - 1].ptr2) return 0;
+    f |= fmk::RT_CONV;
+    if (st.vout.Cc == 1 && st.out_mode == 0 && st.dst_type == FM_C64 &&
+        !st.accumulate)
+      f |= fmk::RT_DIRECT;
+    return f;
+  }
+  return 0;
+}
+
 class Planner {
  public:
   Planner(fm_plan *P, const std::vector<NodeRec> &nodes)
@@ -1771,6 +1826,24 @@ class Planner {
     ls.ept = odd ? ept_ / 2 : ept_;
     if (!configure(P_->esz, ls, 0, 0))
       fail(FM_ERR_UNSUPPORTED, "working length too large for one tile");
+    if (P_->ctype == FM_C64 && ls.kind == 0 && rtile_shape(ls.st)) {
+      // a register tile program (fm_rtile.cuh) runs on vector-major tiles
+      // that give every thread its 8 points (the autotuner may still pick
+      // another layout, which then runs the stage program)
+      int wantB = 0;
+      for (int b = 1; b <= 1024; b *= 2) {
+        LStep t = ls;
+        if (!configure(P_->esz, t, b, 0, false, 0, false)) continue;
+        if (t.threads > FM_MAX_THREADS ||
+            fmk::tile_bytes(b, t.st.Lp, P_->esz) > (size_t)48 * 1024)
+          break;
+        wantB = b;
+      }
+      LStep t = ls;
+      if (wantB && configure(P_->esz, t, wantB, 0, false, 0, false) &&
+          rtile_threads_ok(t))
+        ls = t;
+    }
   }
 
   fmk::Step base_step() {
@@ -2179,6 +2252,9 @@ void launch_step(fm_plan *P, LStep &ls, fmk::Step &st, cudaStream_t s) {
     return;
   }
   P->pair_done = false;
+  st.rprog = 0;
+  if (ls.kind == 0 && P->ctype == FM_C64 && rtile_threads_ok(ls))
+    st.rprog = rtile_shape(st);
   if (ls.kind == 3) {
     // raw buffers of the I/O type; the contiguous kernel also wants
     // 16-byte aligned columns and vectors
@@ -3116,54 +3192,6 @@ int fm_plan_describe(const fm_plan *plan, int32_t direction, char *buf,
     buf[n] = 0;
     return FM_OK;
   });
-}
-
-// The register tile program (fm_rtile.cuh) a complex64 batch step runs, or
-// 0 when its vector program is not one of the shapes it covers:
-// [zero pad] DIF(L) [twiddle] or [zero pad] DIF(L) product DIT(L) [twiddle],
-// L = 64 .. 512 with the radix sequence (8, 8, ..., rest).
-static int rtile_shape(const fmk::Step &st) {
-  const int L = st.L;
-  if (L != 64 && L != 128 && L != 256 && L != 512) return 0;
-  if (st.out_mode == 1 || st.nops < 1) return 0;
-  auto radices_ok = [&](const fmk::Op &op) {
-    if (op.len != L || op.nrad != fmk::rc_stages(L, fmk::kRtP)) return false;
-    for (int i = 0; i < op.nrad; ++i)
-      if (op.rad[i] != fmk::rc_radix(i, L, fmk::kRtP)) return false;
-    return true;
-  };
-  int f = 0, o = 0, end = st.nops;
-  if (st.ops[0].kind == fmk::OP_ZPAD) {
-    if (st.ops[0].len2 != L || st.ops[0].len > L) return 0;
-    f |= fmk::RT_ZPAD;
-    o = 1;
-  }
-  if (end > o + 1 && st.ops[end - 1].kind == fmk::OP_TW) {
-    const fmk::Op &t = st.ops[end - 1];
-    if (t.len != L || t.N <= 0 || t.div < 1 || t.mod < 1 || !t.ptr3)
-      return 0;
-    f |= fmk::RT_TW;
-    --end;
-  }
-  if (o >= end) return 0;
-  const fmk::Op &d = st.ops[o];
-  if (d.kind != fmk::OP_DIF || !radices_ok(d)) return 0;
-  if (end == o + 1) {
-    if ((f & fmk::RT_TW) && !st.ops[st.nops - 1].ptr2) return 0;
-    return f | fmk::RT_FFT | (d.sign > 0 ? fmk::RT_INV : 0);
-  }
-  if (end == o + 3 && st.ops[o + 1].kind == fmk::OP_MUL &&
-      st.ops[o + 1].len == L && st.ops[o + 1].div >= 1 &&
-      st.ops[o + 1].mod >= 1 && st.ops[o + 2].kind == fmk::OP_DIT &&
-      radices_ok(st.ops[o + 2]) && d.sign < 0 && st.ops[o + 2].sign > 0) {
-    if ((f & fmk::RT_TW) && st.ops[st.nops - 1].ptr2) return 0;
-    f |= fmk::RT_CONV;
-    if (st.vout.Cc == 1 && st.out_mode == 0 && st.dst_type == FM_C64 &&
-        !st.accumulate)
-      f |= fmk::RT_DIRECT;
-    return f;
-  }
-  return 0;
 }
 
 int fm_batch_create(int32_t num_ops, fm_plan *const *plans,

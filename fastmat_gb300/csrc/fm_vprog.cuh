@@ -1198,10 +1198,10 @@ template <class E, int LAY>
 __device__ __forceinline__ void store_fixup_vm(const Step &p, E *sm,
                                                const VInfo *vi,
                                                const int *sexp, int tid,
-                                               int T) {
+                                               int T, bool natural = false) {
   const int B = p.B, Lp = p.Lp, n = p.out_len;
   const int total = B * n;
-  if (p.out_pos) {
+  if (p.out_pos && !natural) {
     constexpr int MB = Ept<E>::v;
     E v[MB];
     {
@@ -1653,6 +1653,10 @@ __device__ __forceinline__ void run_program(const Step &p, E *sm, int Lp,
   }
 }
 
+}  // namespace fmk
+#include "fm_rtile.cuh"
+namespace fmk {
+
 // polls of a bounded mbarrier wait before a launch reports FM_ERR_TIMEOUT
 // (the default of Step::wait_limit; fm_plan_set_wait_limit changes it)
 #define FM_WAIT_LIMIT (1LL << 22)
@@ -1810,7 +1814,18 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       __syncthreads();
     }
 
-    if (wmode) {
+    bool natural = false, stored = false;
+    if constexpr (std::is_same<E, float2>::value && LAY == 0) {
+      if (p.rprog) {
+        // the program on registers (fm_rtile.cuh); results in natural
+        // order, or already stored
+        rt_program(p, sm, vi, tid, T);
+        natural = true;
+        stored = (p.rprog & RT_DIRECT) != 0;
+      }
+    }
+    if (natural) {
+    } else if (wmode) {
       // each warp runs the program on its own B / nwarps vectors
       const int w = tid >> 5, vw = B / nwarps;
       run_program<E, CLS, LAY>(p, sm + w * vw * Lp, Lp, vw, vi + w * vw,
@@ -1820,7 +1835,8 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       run_program<E, CLS, LAY>(p, sm, Lp, B, vi, sq, tid, T, tc, &tds);
     }
 
-    if (tma_out) {
+    if (stored) {
+    } else if (tma_out) {
       if constexpr (LAY == 1) {
         store_fixup_em<E>(p, sm, vi, tid, T);
         if constexpr (Emu<E>::v) {
@@ -1828,7 +1844,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
           __syncthreads();
         }
       } else {
-        store_fixup_vm<E, LAY>(p, sm, vi, sexp, tid, T);
+        store_fixup_vm<E, LAY>(p, sm, vi, sexp, tid, T, natural);
       }
       // every writer orders its shared-memory writes before the bulk /
       // TMA reads of the store, then the issuing threads start it
@@ -1836,7 +1852,7 @@ __global__ void __launch_bounds__(FM_MAX_THREADS, (MinBlocks<E, CLS>::v))
       __syncthreads();
       issue_store<E, LAY>(p, sm, tile, dV, nvec, tid, T);
     } else {
-      store_tile<E, LAY>(p, sm, vi, sexp, tid, T);
+      store_tile<E, LAY>(p, sm, vi, sexp, tid, T, natural);
     }
     if (tma_in) {
       // refill the buffer freed one iteration ago (tile - G) with the tile
@@ -1932,9 +1948,6 @@ __host__ __device__ __forceinline__ size_t batch_smem(int max_B,
   return batch_head_bytes(max_B) + 2 * max_tile;
 }
 
-}  // namespace fmk
-#include "fm_rtile.cuh"
-namespace fmk {
 
 // Loads of one batch tile into a slot: cp.async when the source already
 // has the compute type and needs no gather (completion is awaited later,
