@@ -257,10 +257,11 @@ struct LStep {
   int kind = 0;
   int rc_L = 0;
   // kind 3: the real type the FWHT kernel runs in (complex data as pairs
-  // of real vectors), and for strided vectors their element stride, count
-  // per column and column strides in real words (0: contiguous kernel)
+  // of real vectors), and for strided vectors their element stride and
+  // count per column in real words (rc_es 0: contiguous kernel); kind 4:
+  // the same stride and count in elements
   int rc_ct = 0;
-  i64 rc_es = 0, rc_A = 0, rc_ld_src = 0, rc_ld_dst = 0;
+  i64 rc_es = 0, rc_A = 0;
   // two-pass FWHT run as one launch (rfwht2_kernel): 1 on the contiguous
   // pass, which then also runs the strided pass that follows it (its length,
   // element stride and vectors per column in rc2_*), 2 on that strided pass
