@@ -360,7 +360,9 @@ def roofline_of(fg, plan, per_launch, n_in, n_out, M, dt, out_dt, peak,
     ach = lb[k] / (per_launch[k] * 1e-3) / 1e9
     line = [ln for ln in plan.describe(0).splitlines()
             if ln.startswith('launch')][k]
-    if 'rconv' in line:
+    if 'rconv' in line and 'fused-with-next' in line:
+        kernel = 'rkch (circulant and Hadamard modes, one launch)'
+    elif 'rconv' in line:
         kernel = 'rconv'
     elif 'fused-with-next' in line:
         kernel = 'rfwht2 (both FWHT passes, one launch)'

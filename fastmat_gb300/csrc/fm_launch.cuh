@@ -8,6 +8,7 @@
 #include "fm_rconv.cuh"
 #include "fm_rfwht.cuh"
 #include "fm_rsfft.cuh"
+#include "fm_rpair.cuh"
 #include "fm_vprog.cuh"
 
 namespace fmk {
@@ -75,6 +76,12 @@ int rsfwht_max_len(int ctype);
 int rsfft_min_len(int ctype);
 int rsfft_max_len(int ctype);
 cudaError_t launch_rsfft(int ctype, const RsfStep &p, cudaStream_t s);
+// a circulant Kron mode and the Hadamard mode after it in one launch
+// (rkch_kernel): whether it is built for the lengths and a block's items
+// divide evenly (n1 / n2: convolution / FWHT items per block)
+bool rkch_supported(int ctype, int L1, int L2, i64 block_rows,
+                    i64 real_per_block, int *n1, int *n2);
+cudaError_t launch_rkch(int ctype, const RchPair &p, cudaStream_t s);
 // both passes of a two-pass FWHT in one launch (rfwht2_kernel)
 bool rfwht2_supported(int ctype, int L1, int L2);
 cudaError_t launch_rfwht2(int ctype, const RfPair &p, cudaStream_t s);
