@@ -2976,10 +2976,13 @@ int fm_execute_host(fm_plan *plan, int32_t direction, const void *x,
       // (the chunks run their fused pairs as separate launches: with the
       // fused launches inside this pipeline the Kron call measured 19.8
       // against 7.4 ms)
-      plan->no_pair = true;
+      struct NoPair {  // reset also when run_plan throws
+        fm_plan *p;
+        explicit NoPair(fm_plan *q) : p(q) { p->no_pair = true; }
+        ~NoPair() { p->no_pair = false; }
+      } no_pair(plan);
       const int s2 = run_plan(plan, direction, dxk, x_type, ld_x, dyk, y_type,
                               ld_y, m, hs.comp);
-      plan->no_pair = false;
       if (s2 != FM_OK) return s2;
       CUDA_TRY(cudaEventRecord(ev_done, hs.comp));
       CUDA_TRY(cudaStreamWaitEvent(hs.out, ev_done, 0));
